@@ -1,0 +1,489 @@
+"""Throughput of the D3Q19 + coffee-particle hot path on GB300 (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the coupled FP32 case): 128^3 D3Q19, Smagorinsky LES (Cs 0.1, local strain), 3-cell
+porous filter band (eps 0.6, K 1e-3, C_F 0.55), V60 cone with drain hole and inlet disk,
+Guo gravity, 20,000 log-normal particles (median d 0.6 cells, sigma 0.35, density ratio 1.2)
+two-way coupled.  One step = particle coupling (gather/drag/relax/spread/integrate, cell sort
+every 20 steps) + one fused LBM step.  MLUPS = cells x steps / time (all cells, as the
+reference's benchmark_suite.py:129).  Inputs are seeded synthetic (no dataset exists).
+
+`value` replays CUDA graphs of 20 coupled steps with all state resident in HBM; `e2e` drives
+the public solver API step by step with a host-to-device copy of the pour control (17 floats)
+and a device-to-host copy of the step's FP64 sums every step.  `roofline` times the dominant
+kernel (the fused LBM step with its particle-force read and u write) alone with CUDA events.
+Extra lines: 256^3 FP32 / FP16S / BF16S storage (LES + porous band, no particles).
+The reference arm (--impl reference) times the CPU restatement of the same workload on the
+host cores (the reference itself is Python + Taichi and cannot run here).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FALLBACK_HBM_GBS = 6800.0
+GRAPH_STEPS = 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extra", action="store_true", help="skip the 256^3 precision lines")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--error-steps", type=int, default=2000, help="steps of the FP64 error runs")
+    ap.add_argument("--small", action="store_true", help="64^3 / 2,000 particles (profiling)")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for name, v in zip(names[1:], r[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def workload(small=False):
+    from pour_over_coffee_lbm_gb300.params import coupled_128
+    cfg, pc = coupled_128()
+    if small:
+        cfg = cfg.replace(nx=64, ny=64, nz=64)
+        pc.count = 2000
+    return cfg, pc
+
+
+def fluid_cells(flags):
+    import torch
+    from pour_over_coffee_lbm_gb300.params import CELL_SOLID
+    return int(((flags & CELL_SOLID) == 0).sum().item())
+
+
+def time_graph(graph, replays):
+    import torch
+    stream = torch.cuda.current_stream()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(replays):
+        graph.replay()
+    end.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / 1e3
+
+
+def kernel_roofline(cfg, steps, peak):
+    """Average duration of the fused LBM step kernel alone (same arguments as inside the coupled
+    step: external force read, rho/u write), over `steps` graph-replayed launches."""
+    import torch
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    s = GB300LBMSolver(cfg)
+    s._force.normal_(0.0, 1e-7)
+    s._force_active = True
+    for _ in range(4):
+        s.run(1, want_macro=True)
+    torch.cuda.synchronize()
+    g = GraphOfSteps(s, GRAPH_STEPS)
+    time_graph(g, 2)
+    reps = max(1, steps // GRAPH_STEPS)
+    dt = time_graph(g, reps)
+    per_launch = dt / (reps * GRAPH_STEPS)
+    nf = fluid_cells(s.flags)
+    esize = s._f.element_size()
+    bytes_per_launch = nf * (2 * 19 * esize + 12 + 4 + 12) + s.n * 1
+    achieved = bytes_per_launch / per_launch / 1e9
+    out = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0], "unit": "GB/s",
+           "frac": round(achieved / peak[0], 4), "peak_source": peak[1],
+           "kernel": "aa_step_kernel (fused collide-stream, force read, rho/u write)",
+           "kernel_us": round(per_launch * 1e6, 2), "algorithmic_bytes_per_launch": bytes_per_launch,
+           "fluid_cells": nf, "cells": s.n}
+    del s, g
+    return out
+
+
+class GraphOfSteps:
+    """CUDA graph of n plain steps with the solver's current force/macro options."""
+
+    def __init__(self, solver, n):
+        import torch
+        self.s = solver
+        self.n = n
+        t0 = solver.t
+        self.g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.g):
+            for _ in range(n):
+                solver.run(1, want_macro=True)
+        solver.t = t0
+
+    def replay(self):
+        self.g.replay()
+        self.s.t += self.n
+
+
+def precision_line(storage, steps, peak):
+    import torch
+    from pour_over_coffee_lbm_gb300.params import precision_256
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    cfg = precision_256(storage=storage)
+    s = GB300LBMSolver(cfg)
+    for _ in range(4):
+        s.run(1)
+    torch.cuda.synchronize()
+    import pour_over_coffee_lbm_gb300._lib as L
+    t0 = s.t
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(GRAPH_STEPS):
+            s.run(1)
+    s.t = t0
+
+    class _G:
+        def replay(self_inner):
+            g.replay()
+            s.t += GRAPH_STEPS
+    gg = _G()
+    time_graph(gg, 2)
+    reps = max(1, steps // GRAPH_STEPS)
+    dt = time_graph(gg, reps)
+    per = dt / (reps * GRAPH_STEPS)
+    nf = fluid_cells(s.flags)
+    esize = s._f.element_size()
+    bpl = nf * 2 * 19 * esize + s.n
+    mlups = s.n / per / 1e6
+    ach = bpl / per / 1e9
+    out = {"mlups": round(mlups, 1), "kernel_us": round(per * 1e6, 2), "achieved_gbs": round(ach, 1),
+           "frac": round(ach / peak[0], 4), "bytes_per_lup": round(bpl / s.n, 2)}
+    del s, g
+    torch.cuda.empty_cache()
+    return out
+
+
+def precision_errors(steps):
+    """u and rho relative L2 error (fluid cells) of FP32 / FP16S / BF16S storage against an FP64
+    run of the same 256^3 case from the same initial state after `steps` steps."""
+    import torch
+    from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32, STORE_F64, precision_256
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    ref = GB300LBMSolver(precision_256(storage=STORE_F64))
+    ref.run(steps - 1)
+    ref.run(1, want_macro=True)
+    fluid = (ref.flags & 1) == 0
+    u64 = ref._u[:, fluid].double().clone()
+    r64 = ref._rho[fluid].double().clone()
+    del ref
+    torch.cuda.empty_cache()
+    out = {"steps": steps}
+    for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
+        s = GB300LBMSolver(precision_256(storage=st))
+        s.run(steps - 1)
+        s.run(1, want_macro=True)
+        u = s._u[:, fluid].double()
+        r = s._rho[fluid].double()
+        out[name] = {"u_rel_l2": float(torch.linalg.norm(u - u64) / torch.linalg.norm(u64)),
+                     "rho_rel_l2": float(torch.linalg.norm(r - r64) / torch.linalg.norm(r64))}
+        del s
+        torch.cuda.empty_cache()
+    return out
+
+
+def cpu_baseline(cfg, pc, seconds):
+    """The CPU restatement (oracle, OpenMP on all host cores, particles serial) on the same
+    workload, time-bounded: returns MLUPS and the sample it measured."""
+    import numpy as np
+    import oracle as O
+    from pour_over_coffee_lbm_gb300.params import seed_particles
+    flags = O.build_flags(cfg)
+    f = O.init_equilibrium(cfg, flags, np.float32)
+    pos, vel, d, act = seed_particles(cfg, pc)
+    drag = np.zeros_like(pos)
+    _, _, u = O.step(cfg, flags, f)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        pos, vel, drag, act, fix, _ = O.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
+        force = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(3, cfg.nz, cfg.ny, cfg.nx)
+        f, rho, u = O.step(cfg, flags, f, force=force)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 500:
+            break
+    return cfg.ncell * steps / el / 1e6, steps, el
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from pour_over_coffee_lbm_gb300 import _lib
+    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    lib = _lib.load()
+    peak = peaks()
+    cfg, pc = workload(args.small)
+    solver = GB300LBMSolver(cfg)
+    ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
+    ps.seed()
+    W = max(3, args.warmup)
+    for _ in range(W):
+        solver.step_with_two_way_coupling(ps)
+    if solver.t % 2:
+        solver.step_with_two_way_coupling(ps)
+    torch.cuda.synchronize()
+    graph = solver.capture(GRAPH_STEPS, ps)
+    graph.replay()
+    torch.cuda.synchronize()
+    K = args.steps
+    reps, rem = divmod(K, GRAPH_STEPS)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(reps):
+        graph.replay()
+    for _ in range(rem):
+        solver.step_with_two_way_coupling(ps)
+    end.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    elapsed = start.elapsed_time(end) / 1e3
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    launches = graph.kernels * reps + (rem * (graph.kernels // GRAPH_STEPS))
+    value = world * cfg.ncell * K / elapsed / 1e6
+    diag = solver.get_diagnostics()
+
+    # end to end through the public API: per step H2D pour control, D2H FP64 sums
+    # one pinned slot per step: an async copy never reads a slot the host is rewriting
+    ctl_h = torch.zeros((K, 17), dtype=torch.float32).pin_memory()
+    for i in range(K):
+        ctl_h[i, 0] = cfg.u_inlet * (1.0 + 0.1 * ((i % 50) / 50.0))  # a slowly varying pour
+    ctl_d = torch.zeros(17, dtype=torch.float32, device="cuda")
+    ctl_d.copy_(ctl_h[0])
+    solver.set_inlet_control(ctl_d)
+    red_h = torch.zeros((K, 6), dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        solver.step_with_two_way_coupling(ps, reduce=True)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for i in range(K):
+        ctl_d.copy_(ctl_h[i], non_blocking=True)
+        red = solver.step_with_two_way_coupling(ps, reduce=True)
+        red_h[i].copy_(red, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_el], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_el = float(t.item())
+    e2e_ok = bool(torch.isfinite(red_h[:, :5]).all()) and float(red_h[:, 5].sum()) == 0.0
+    solver.set_inlet_control(None)
+
+    roof = kernel_roofline(cfg, max(200, K), peak)
+    traffic_path = os.path.join(ROOT, "profiles", "aa_step_traffic.json")
+    roof["traffic"] = None
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as fh:
+            tr = json.load(fh)
+        key = "%dx%dx%d" % (cfg.nx, cfg.ny, cfg.nz)
+        if key in tr:
+            roof["traffic"] = tr[key]["bytes_per_launch"]
+            roof["traffic_source"] = tr[key].get("source")
+
+    extra = None
+    if not args.no_extra and not args.small and rank == 0:
+        from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
+        del graph
+        torch.cuda.empty_cache()
+        p32 = precision_line(STORE_F32, 200, peak)
+        p16 = precision_line(STORE_F16S, 200, peak)
+        pb16 = precision_line(STORE_BF16S, 200, peak)
+        errs = precision_errors(args.error_steps)
+        extra = {"workload": "256^3 D3Q19 + LES(local) + porous band, no particles",
+                 "fp32": p32, "fp16s": p16, "bf16s": pb16, "error_vs_fp64": errs,
+                 "fp16s_vs_fp32_mlups": round(p16["mlups"] / p32["mlups"], 3),
+                 "bf16s_vs_fp32_mlups": round(pb16["mlups"] / p32["mlups"], 3)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        mlups, steps, el = cpu_baseline(cfg, pc, args.cpu_seconds)
+        cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+               "sample": "%d coupled steps of the same %dx%dx%d + %d-particle workload (%.1f s), "
+                         "CPU restatement (OpenMP lattice, serial particles)"
+                         % (steps, cfg.nx, cfg.ny, cfg.nz, pc.count, el)}
+
+    if rank == 0:
+        line = {
+            "metric": "D3Q19 MLUPS & % HBM roofline; FP16-store vs FP32 MLUPS at <=1e-3 rel err",
+            "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": round(elapsed * 1e3 / K, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded V60 geometry and particles)",
+            "config": {"workload": "coupled FP32: %dx%dx%d D3Q19, LES Cs 0.1 (local strain), porous band 3 cells "
+                                   "(eps 0.6, K 1e-3, C_F 0.55), %d log-normal particles two-way coupled"
+                                   % (cfg.nx, cfg.ny, cfg.nz, pc.count),
+                       "cells": cfg.ncell, "particles": pc.count, "graph_steps": GRAPH_STEPS,
+                       "l2": "distributions %.0f MB > 129 MB L2 (no flush)" % (19 * 4 * cfg.ncell / 1e6),
+                       "parallelism": "replicas x%d (one independent lattice per GPU)" % world},
+            "e2e": {"value": round(world * cfg.ncell * K / e2e_el / 1e6, 1), "unit": "MLUPS",
+                    "h2d_bytes_per_step": 17 * 4, "d2h_bytes_per_step": 6 * 8,
+                    "api": "GB300LBMSolver.step_with_two_way_coupling(reduce=True) per step",
+                    "results_finite": e2e_ok},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "precision_256": extra,
+            "diagnostics": {"mass": diag["mass"], "max_velocity": diag["max_velocity"], "stable": diag["stable"]},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    cfg, pc = workload(args.small)
+    # each step of this arm is one coupled step of the CPU restatement; the run is bounded to
+    # about two minutes by timing at most the steps that fit (reported in `sample`)
+    import numpy as np
+    import oracle as O
+    from pour_over_coffee_lbm_gb300.params import seed_particles
+    flags = O.build_flags(cfg)
+    f = O.init_equilibrium(cfg, flags, np.float32)
+    pos, vel, d, act = seed_particles(cfg, pc)
+    drag = np.zeros_like(pos)
+    _, _, u = O.step(cfg, flags, f)
+
+    def one():
+        nonlocal pos, vel, drag, act, f, u
+        pos, vel, drag, act, fix, _ = O.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
+        force = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(3, cfg.nz, cfg.ny, cfg.nx)
+        f, _, u = O.step(cfg, flags, f, force=force)
+
+    W = max(3, args.warmup)
+    t0 = time.perf_counter()
+    one()
+    per = time.perf_counter() - t0
+    wsteps = min(W, max(1, int(20.0 / per)))
+    for _ in range(wsteps - 1):
+        one()
+    K = args.steps
+    k_run = min(K, max(3, int(120.0 / per)))
+    t0 = time.perf_counter()
+    for _ in range(k_run):
+        one()
+    el = time.perf_counter() - t0
+    mlups = cfg.ncell * k_run / el / 1e6
+    line = {"impl": "reference",
+            "metric": "D3Q19 MLUPS & % HBM roofline; FP16-store vs FP32 MLUPS at <=1e-3 rel err",
+            "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": round(el * 1e3 / k_run, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded V60 geometry and particles)",
+            "config": {"workload": "coupled FP32: %dx%dx%d D3Q19, LES Cs 0.1 (local strain), porous band 3 cells "
+                                   "(eps 0.6, K 1e-3, C_F 0.55), %d log-normal particles two-way coupled"
+                                   % (cfg.nx, cfg.ny, cfg.nz, pc.count)},
+            "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+                             "sample": "%d of %d requested coupled steps timed (%.1f s); the reference is "
+                                       "Python+Taichi (not installable here), this is its CPU restatement"
+                                       % (k_run, K, el)},
+            "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,246 @@
+/*
+ * pog.h -- C ABI of libpog.so, the GB300 (sm_103a) D3Q19 lattice-Boltzmann step and
+ * Lagrangian coffee-particle coupling of the pour-over V60 simulator.
+ *
+ * The reference (latteine1217/pour-over-coffee-lbm) is Python + Taichi and has no FFI: its
+ * "operator API" is the solver object (src/core/lbm_protocol.py:12-238, the legacy
+ * LBMSolver in src/core/legacy/lbm_solver.py and CoffeeParticleSystem in
+ * src/physics/coffee_particles.py).  Each entry point below replaces one Taichi kernel (or a
+ * fused group of them) of that object; the replaced reference code is cited beside it.  The
+ * Python package pour_over_coffee_lbm_gb300 binds these with ctypes and exposes the
+ * reference's solver protocol and accessors on top.
+ *
+ * Conventions
+ *   - Every pointer argument is caller-owned DEVICE memory (for example a torch CUDA
+ *     tensor) unless the comment says "host".  The library allocates no device memory.
+ *   - Fields are structure-of-arrays with x fastest: cell index c = (k*ny + j)*nx + i, a
+ *     distribution array is f[q*ncell + c], a vector field is v[a*ncell + c] (a = x,y,z).
+ *   - Calls are stream-ordered on the cudaStream_t passed as `stream` (0 = legacy default
+ *     stream).  Nothing synchronises the host unless stated.
+ *   - Return value: 0 (POG_OK) on success, a negative POG_E_* code on failure; the message
+ *     is available from pog_last_error() (thread-local).  No exception crosses the ABI and
+ *     the library never exits the process.
+ *   - D3Q19 ordering is the reference's config/core.py:36-47 ordering; opposite(q) is
+ *     {0,2,1,4,3,6,5,10,9,8,7,14,13,12,11,18,17,16,15} (legacy/lbm_solver.py:431-439).
+ */
+#ifndef POG_H
+#define POG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define POG_VERSION 1
+
+/* ---- error codes ---------------------------------------------------------------------- */
+#define POG_OK 0
+#define POG_E_ARG (-1)      /* invalid argument (null pointer, bad size, bad enum)         */
+#define POG_E_CUDA (-2)     /* a CUDA runtime call failed                                    */
+#define POG_E_NAN (-3)      /* a non-finite density or velocity was detected                 */
+#define POG_E_INJECTED (-4) /* host-side fault injection (POG_FAULT_INJECT_STEP) fired       */
+#define POG_E_RANGE (-5)    /* a size is beyond a documented limit                           */
+#define POG_E_STATE (-6)    /* call sequence error (e.g. odd AA parity where even required)  */
+
+/* ---- cell flag bits (one uint8 per cell) ------------------------------------------------- */
+#define POG_CELL_SOLID 0x01u      /* half-way bounce-back wall (filter_paper.py:206-286)     */
+#define POG_CELL_INLET 0x02u      /* fixed-velocity inlet disk (equilibrium at rho_local)    */
+#define POG_CELL_OUTLET 0x04u     /* pressure outlet under the apex hole (equilibrium rho_out)*/
+#define POG_CELL_POROUS 0x08u     /* filter-paper band: Darcy-Forchheimer drag, LES off      */
+#define POG_CELL_NEAR_SOLID 0x10u /* at least one of the 18 neighbours is solid              */
+
+/* ---- enums -------------------------------------------------------------------------------- */
+enum pog_storage {     /* how the distributions are stored in HBM                           */
+  POG_STORE_F32 = 0,   /* float f_i                                                          */
+  POG_STORE_F16S = 1,  /* IEEE half of (f_i - w_i*rho0); collision in FP32                   */
+  POG_STORE_BF16S = 2, /* bfloat16 of (f_i - w_i*rho0); collision in FP32                    */
+  POG_STORE_F64 = 3    /* double f_i, collision in FP64 (reference runs for error reports)  */
+};
+enum pog_les_mode {
+  POG_LES_OFF = 0,
+  POG_LES_STENCIL = 1, /* |S| by central differences of the previous step's u
+                          (les_turbulence.py:318-380); needs the u ping-pong buffers         */
+  POG_LES_LOCAL = 2    /* |S| from the local non-equilibrium stress (Hou et al. 1996)         */
+};
+enum pog_drag_mode {
+  POG_DRAG_SEMI_IMPLICIT = 0, /* velocity solved with the drag (Guo & Zhao 2002)             */
+  POG_DRAG_EXPLICIT_CAP = 1   /* reference form: drag from the force-free velocity, |F| capped
+                                 (filter_paper.py:471-536)                                    */
+};
+enum pog_forcing_mode {
+  POG_FORCING_GUO = 0,       /* standard Guo 2002 (docs/mathematical/mathematical_models.md)  */
+  POG_FORCING_REFERENCE = 1  /* legacy form 3e.F + 9(e.u)(u.F) with its clamps
+                                (legacy/lbm_solver.py:594-607,688-764)                        */
+};
+
+#define POG_INLET_NCOEF 16
+
+/* Run-time parameters of one lattice (lattice units throughout).  Field names follow the
+ * reference's config names where one exists (config/core.py, config/physics.py). */
+typedef struct pog_params {
+  int32_t nx, ny, nz;       /* NX, NY, NZ                                                     */
+  int32_t storage;          /* enum pog_storage                                               */
+  int32_t les_mode;         /* enum pog_les_mode                                              */
+  int32_t drag_mode;        /* enum pog_drag_mode                                             */
+  int32_t forcing_mode;     /* enum pog_forcing_mode                                          */
+  int32_t clamp_tau;        /* 1: clamp tau_eff into [tau_min, tau_max] (lbm_solver.py:571)   */
+  float tau;                /* molecular relaxation time (TAU_WATER)                          */
+  float rho0;               /* reference density, also the storage shift                     */
+  float gx, gy, gz;         /* gravity acceleration; force density is rho*g                   */
+  float cs_smag;            /* Smagorinsky constant (SMAGORINSKY_CONSTANT)                    */
+  float les_strain_floor;   /* |S| below which nu_sgs = 0 (reference 1e-3)                    */
+  float les_nu_max;         /* upper clamp of nu_sgs (reference 0.1)                           */
+  float tau_min, tau_max;   /* tau_eff clamp when clamp_tau (reference 0.55, 1.90)            */
+  /* V60 geometry (filter_paper.py:206-364), lattice units */
+  float cone_apex_z;        /* z of the cone apex                                             */
+  float cone_half_angle_deg;/* half angle of the cone                                         */
+  float cone_wall;          /* horizontal wall thickness                                      */
+  float hole_radius;        /* radius of the drain hole through the apex                      */
+  float inlet_radius;       /* radius of the inlet disk on plane k = nz-2                     */
+  float band_thickness;     /* filter-paper band thickness inside the wall (0 = none)         */
+  float center_x, center_y; /* cone axis; negative = nx*0.5, ny*0.5 (filter_paper.py:229)     */
+  /* filter-paper porous band (filter_paper.py:423-536) */
+  float porosity;           /* eps0 at which permeability/forchheimer are quoted              */
+  float permeability;       /* Darcy permeability K0 (lattice units)                          */
+  float forchheimer;        /* Forchheimer coefficient C_F0                                   */
+  float drag_cap;           /* |F_drag| cap in POG_DRAG_EXPLICIT_CAP mode                      */
+  /* inlet / outlet */
+  float u_inlet;            /* base inlet velocity u_z (negative = downward)                   */
+  float inlet_coef[POG_INLET_NCOEF]; /* radial profile: u_z(r) = u_inlet*(1 + sum a_k T_k(2r/R-1)) */
+  float rho_outlet;         /* density imposed on outlet cells                                */
+  /* Optional DEVICE pointer to a pour-control block [u_inlet, a_0 .. a_15] (17 floats) that
+   * overrides u_inlet/inlet_coef when non-null, so a time-varying pour is fed by one small
+   * host-to-device copy per step (and survives CUDA-graph replay).  NULL = use the fields. */
+  const float* inlet_control;
+} pog_params;
+
+/* Reduction slots written by pog_step when `reductions` is non-null (FP64, accumulated with
+ * atomics: zero them before a call to get that call's sums).  Replaces the host-side np.sum
+ * conservation checks of src/visualization/lbm_diagnostics.py:228-291. */
+#define POG_RED_MASS 0      /* sum over fluid cells of rho                                   */
+#define POG_RED_MOMX 1      /* sum of rho*u_x                                                */
+#define POG_RED_MOMY 2
+#define POG_RED_MOMZ 3
+#define POG_RED_OUTFLOW 4   /* outflow mass flux: -sum over outlet cells of sum_i c_iz f_i   */
+#define POG_RED_NONFINITE 5 /* number of cells whose rho or u is not finite                  */
+#define POG_RED_COUNT 6
+
+/* Particle-model parameters (coffee_particles.py:1048-1212, 641-831). */
+typedef struct pog_particle_params {
+  float density_ratio;  /* rho_p / rho0                                                       */
+  float relaxation;     /* under-relaxation alpha of the drag force (lbm_solver.py:1485: 0.8)  */
+  float dt;             /* particle time step (lattice units)                                 */
+  int32_t drag_model;   /* 0 Stokes, 1 Schiller-Naumann correction (coffee_particles.py:1088)  */
+  int32_t deterministic;/* 1: fixed-point integer accumulation of the spread force            */
+  float wall_margin;    /* radial limit as a fraction of the cone radius (0.9)                 */
+  float wall_pullback;  /* radius a violating particle is moved to, fraction (0.8)             */
+  float wall_damping;   /* velocity factor on a wall hit (0.3)                                 */
+  float z_floor;        /* particles are kept above cone_apex_z + z_floor                      */
+} pog_particle_params;
+
+/* ---- library ------------------------------------------------------------------------------- */
+int pog_version(void);
+const char* pog_last_error(void);
+/* Number of kernel launches this thread issued through the library since the last reset. */
+long long pog_launch_count(int reset);
+
+/* Check a parameter block (sizes, enum values, ranges).  Host only. */
+int pog_validate_params(const pog_params* p);
+
+/* ---- geometry ------------------------------------------------------------------------------ */
+/* Build the uint8 cell flags of the V60 mask, drain hole, inlet/outlet disks and porous band.
+ * Replaces FilterPaperSystem._setup_v60_geometry / _setup_filter_zones
+ * (filter_paper.py:206-364) and the LES mask copy (filter_paper.py:199-204).  Computed in FP64
+ * without contraction: the result is bit-exact with the CPU restatement. */
+int pog_build_flags(const pog_params* p, uint8_t* flags, void* stream);
+
+/* ---- distributions --------------------------------------------------------------------------- */
+/* f := equilibrium(rho0, u0) on every non-solid cell, 0 on solid cells, in the storage format
+ * of p->storage.  The state is left at AA parity 0 (natural layout).
+ * Replaces LBMSolver.init_fields (legacy/lbm_solver.py:1067-1112). */
+int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, float rho0,
+                         float ux, float uy, float uz, void* stream);
+
+/* Advance `nsteps` time steps in place (AA pattern: one distribution buffer).  `t` is the time
+ * index of the incoming state; its parity selects the AA read/write pattern.  Each step is
+ * LBMSolver.step (legacy/lbm_solver.py:817-867): macroscopic moments (:488-535), Guo forcing
+ * (:594-607,688-764), LES relaxation (les_turbulence.py:289-380), BGK collision and push
+ * streaming with half-way bounce-back (:537-628), the filter-band Darcy-Forchheimer drag
+ * (filter_paper.py:471-536), the particle reaction force (:1478-1483) and the inlet/outlet
+ * boundary overwrite (boundary_conditions.py:384-409), fused into one pass per step.
+ *   force      [3][ncell] external force density (particle reaction, plugins) or NULL
+ *   porosity   [ncell] per-cell eps for porous cells, or NULL (uniform p->porosity)
+ *   u_prev/u_next [3][ncell] velocity ping-pong buffers: required for POG_LES_STENCIL (step s
+ *              reads u_prev and writes u_next; the pointers are swapped every step inside
+ *              the call; after an odd nsteps the newest u is in u_next, else in u_prev)
+ *   rho_out, u_out  macroscopic output (rho and Guo-corrected u of the incoming state) of
+ *              the LAST step, or NULL
+ *   reductions POG_RED_COUNT doubles accumulated over all nsteps, or NULL */
+int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, int nsteps,
+             const float* force, const float* porosity, float* u_prev, float* u_next,
+             float* rho_out, float* u_out, double* reductions, void* stream);
+
+/* Same step on the natural (two-buffer) layout: reads f_in at time t, writes f_out at t+1
+ * with push streaming exactly as legacy/lbm_solver.py:609-628.  Used for checkpointed
+ * recomputation under the adjoint and for FP64 reference runs. */
+int pog_step_push(const pog_params* p, const void* f_in, void* f_out, const uint8_t* flags,
+                  const float* force, const float* porosity, const float* u_prev,
+                  float* rho_out, float* u_out, double* reductions, void* stream);
+
+/* Copy the AA state at time t into natural layout (f_nat[q][c] = f_q at cell c), converting
+ * the storage format to `out_storage` (POG_STORE_F32 or POG_STORE_F64). */
+int pog_export_natural(const pog_params* p, const void* f, const uint8_t* flags, long long t,
+                       void* f_nat, int out_storage, void* stream);
+/* Inverse at an even t: natural FP32/FP64 -> AA state in p->storage. */
+int pog_import_natural(const pog_params* p, const void* f_nat, int in_storage,
+                       const uint8_t* flags, void* f, void* stream);
+
+/* Density and Guo-corrected velocity of the AA state at time t, without advancing it.
+ * Replaces LBMSolver._compute_macroscopic_quantities (legacy/lbm_solver.py:488-535). */
+int pog_macroscopic(const pog_params* p, const void* f, const uint8_t* flags, long long t,
+                    const float* force, float* rho_out, float* u_out, void* stream);
+
+/* ---- particles ----------------------------------------------------------------------------- */
+/* Cell key of every particle, key = i + nx*(j + ny*k) with (i,j,k) = int(clamp(pos, 0, n-2))
+ * (coffee_particles.py:1162-1164); inactive particles get key = ncell.  `perm` receives the
+ * stable ascending order of the keys (equal to numpy.argsort(keys, kind="stable")).
+ * `scratch` must hold pog_particles_bin_scratch_bytes(np) bytes of device memory. */
+size_t pog_particles_bin_scratch_bytes(int np);
+int pog_particles_bin(const pog_params* p, const float* pos, const int32_t* active, int np,
+                      int32_t* keys, int32_t* perm, void* scratch, void* stream);
+
+/* One two-way coupling pass (LBMSolver.step_with_two_way_coupling, legacy/lbm_solver.py:
+ * 1485-1509, with CoffeeParticleSystem.compute_two_way_coupling_forces 1107-1154,
+ * apply_under_relaxation 1200-1212 and update_particle_physics 641-720): for each active
+ * particle, trilinear u at its position, drag, under-relaxation of the drag, spreading of the
+ * relaxed reaction -F onto the 8 surrounding nodes, then velocity/position update with the
+ * cone constraint.  `order` (nullable) lists the particles in processing order (the `perm` of
+ * pog_particles_bin) so neighbouring lanes hit neighbouring cells.
+ *   force     [3][ncell] float accumulator (fast mode; caller zeroes it), or
+ *   force_fix [3][ncell] int64 fixed-point accumulator, scale 2^32 (deterministic mode) */
+int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, float* pos,
+                         float* vel, const float* diameter, float* drag_old, int32_t* active,
+                         int np, const int32_t* order, const float* u, float* force,
+                         long long* force_fix, float* u_at_particle, void* stream);
+/* force[a][c] = force_fix[a][c] * 2^-32 (deterministic-mode conversion). */
+int pog_force_from_fixed(const pog_params* p, const long long* force_fix, float* force,
+                         void* stream);
+
+/* ---- adjoint --------------------------------------------------------------------------------- */
+/* Reverse of one pog_step_push step (natural layout, storage F32 or F64).
+ *   f_t       forward state at time t (natural), the input of the step being reversed
+ *   lam_next  adjoint of the state at t+1;  lam_t  receives the adjoint at t
+ *   The loss is J = sum_t flux_t with flux_t = POG_RED_OUTFLOW of step t, so each outlet
+ *   cell adds dJ/df_i = -c_iz.  Parameter gradients are accumulated in FP64:
+ *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
+ *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL. */
+int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next, void* lam_t,
+                     const uint8_t* flags, const float* porosity, double* grad_porosity,
+                     double* grad_inlet, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POG_H */

@@ -1,0 +1,245 @@
+"""CPU oracle of the hot path -- TEST INFRASTRUCTURE ONLY.
+
+numpy/ctypes front of oracle/_build/liborc.so (built from pog_oracle.cpp and
+pog_oracle_particles.cpp by oracle/build.py).  Imported only by tests/, by
+__graft_entry__.smoke() and by bench.py's CPU-baseline leg; the product never imports it.
+Arrays use the product's layout: x fastest, distributions [19, NZ, NY, NX], vectors
+[3, NZ, NY, NX].
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+_v = ctypes.c_void_p
+_i = ctypes.c_int
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def load():
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            lib = ctypes.CDLL(path)
+            for name in ("orc_build_flags", "orc_init_equilibrium_f32", "orc_step_f32",
+                         "orc_step_f64", "orc_les_nu_f32", "orc_porous_force_f32",
+                         "orc_particles_bin", "orc_particles_couple", "orc_trilinear_f32",
+                         "orc_adjoint_step_f64", "orc_d3q19_tables"):
+                getattr(lib, name).restype = _i
+            lib.orc_init_equilibrium_f64.restype = _i
+            lib.orc_init_equilibrium_f64.argtypes = [_v, _v, _v, ctypes.c_double, ctypes.c_double,
+                                                     ctypes.c_double, ctypes.c_double]
+            lib.orc_init_equilibrium_f32.argtypes = [_v, _v, _v, ctypes.c_float, ctypes.c_float,
+                                                     ctypes.c_float, ctypes.c_float]
+            lib.orc_equilibrium_f64.argtypes = [ctypes.c_double] * 4 + [_v]
+            lib.orc_equilibrium_f32.argtypes = [ctypes.c_float] * 4 + [_v]
+            lib.orc_moments_f64.argtypes = [_v, _v, _v]
+            lib.orc_under_relax.argtypes = [ctypes.c_float, _v, _v, _v, _i]
+            lib.orc_trilinear_f32.argtypes = [_i, _i, _i, _v, _v, _i, _v]
+            lib.orc_round_storage.restype = ctypes.c_float
+            lib.orc_round_storage.argtypes = [_i, ctypes.c_float, _i, ctypes.c_float]
+            lib.orc_inlet_velocity_f64.argtypes = [_v, _v, _v, _i]
+            _lib = lib
+        return _lib
+
+
+def _params(cfg):
+    p = cfg.to_c()
+    return p, ctypes.byref(p)
+
+
+def tables():
+    lib = load()
+    cx = np.zeros(19, np.int32); cy = np.zeros(19, np.int32); cz = np.zeros(19, np.int32)
+    opp = np.zeros(19, np.int32); w = np.zeros(19, np.float64)
+    lib.orc_d3q19_tables(_p(cx), _p(cy), _p(cz), _p(opp), _p(w))
+    return cx, cy, cz, opp, w
+
+
+def build_flags(cfg) -> np.ndarray:
+    lib = load()
+    _, pp = _params(cfg)
+    flags = np.zeros((cfg.nz, cfg.ny, cfg.nx), np.uint8)
+    lib.orc_build_flags(pp, _p(flags))
+    return flags
+
+
+def init_equilibrium(cfg, flags, dtype=np.float64, rho0=None, u0=(0.0, 0.0, 0.0)):
+    lib = load()
+    _, pp = _params(cfg)
+    f = np.zeros((19, cfg.nz, cfg.ny, cfg.nx), dtype)
+    r = cfg.rho0 if rho0 is None else rho0
+    if dtype == np.float64:
+        lib.orc_init_equilibrium_f64(pp, _p(flags), _p(f), r, *u0)
+    else:
+        lib.orc_init_equilibrium_f32(pp, _p(flags), _p(f), r, *u0)
+    return f
+
+
+def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None):
+    """One push step.  Returns (f_next, rho, u)."""
+    lib = load()
+    _, pp = _params(cfg)
+    dt = f.dtype
+    fo = f.copy()
+    rho = np.zeros((cfg.nz, cfg.ny, cfg.nx), dt)
+    u = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), dt)
+    if force is not None:
+        force = np.ascontiguousarray(force, np.float32)
+    if eps is not None:
+        eps = np.ascontiguousarray(eps, np.float32)
+    if u_prev is not None:
+        u_prev = np.ascontiguousarray(u_prev, dt)
+    fn = lib.orc_step_f64 if dt == np.float64 else lib.orc_step_f32
+    fn(pp, _p(flags), _p(f), _p(fo), _p(force), _p(eps), _p(u_prev), _p(rho), _p(u), _p(reductions))
+    return fo, rho, u
+
+
+def run(cfg, nsteps, dtype=np.float64, flags=None, force=None, eps=None, reductions=None):
+    """nsteps from equilibrium.  Returns (flags, f, rho, u) of the last step (rho/u are the
+    moments computed inside that step)."""
+    if flags is None:
+        flags = build_flags(cfg)
+    f = init_equilibrium(cfg, flags, dtype)
+    u = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), dtype)
+    rho = None
+    for _ in range(nsteps):
+        f, rho, u_new = step(cfg, flags, f, force=force, eps=eps,
+                             u_prev=u if cfg.les_mode == 1 else None, reductions=reductions)
+        u = u_new
+    return flags, f, rho, u
+
+
+def les_nu(cfg, flags, u):
+    lib = load()
+    _, pp = _params(cfg)
+    u = np.ascontiguousarray(u, np.float32)
+    nu = np.zeros((cfg.nz, cfg.ny, cfg.nx), np.float32)
+    lib.orc_les_nu_f32(pp, _p(flags), _p(u), _p(nu))
+    return nu
+
+
+def porous_force(cfg, flags, rho, u):
+    lib = load()
+    _, pp = _params(cfg)
+    F = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), np.float32)
+    lib.orc_porous_force_f32(pp, _p(flags), _p(np.ascontiguousarray(rho, np.float32)),
+                             _p(np.ascontiguousarray(u, np.float32)), _p(F))
+    return F
+
+
+def equilibrium(rho, u, dtype=np.float64):
+    lib = load()
+    out = np.zeros(19, dtype)
+    if dtype == np.float64:
+        lib.orc_equilibrium_f64(rho, *u, _p(out))
+    else:
+        lib.orc_equilibrium_f32(rho, *u, _p(out))
+    return out
+
+
+def moments(f):
+    lib = load()
+    f = np.ascontiguousarray(f, np.float64)
+    rho = np.zeros(1); u = np.zeros(3)
+    lib.orc_moments_f64(_p(f), _p(rho), _p(u))
+    return float(rho[0]), u
+
+
+def trilinear(u, pos):
+    """u: [3, NZ, NY, NX] float32; pos: (m, 3) float32 -> (m, 3)."""
+    lib = load()
+    u = np.ascontiguousarray(u, np.float32)
+    pos = np.ascontiguousarray(pos, np.float32)
+    out = np.zeros_like(pos)
+    nz, ny, nx = u.shape[1:]
+    lib.orc_trilinear_f32(nx, ny, nz, _p(u), _p(pos), pos.shape[0], _p(out))
+    return out
+
+
+def under_relax(alpha, fnew, fold):
+    lib = load()
+    fnew = np.ascontiguousarray(fnew, np.float32)
+    fold = np.ascontiguousarray(fold, np.float32).copy()
+    out = np.zeros_like(fnew)
+    lib.orc_under_relax(alpha, _p(fnew), _p(fold), _p(out), fnew.size)
+    return out, fold
+
+
+def particles_bin(cfg, pos, active):
+    lib = load()
+    _, pp = _params(cfg)
+    pos = np.ascontiguousarray(pos, np.float32)
+    active = np.ascontiguousarray(active, np.int32)
+    n = active.shape[0]
+    keys = np.zeros(n, np.int32)
+    perm = np.zeros(n, np.int32)
+    lib.orc_particles_bin(pp, _p(pos), _p(active), n, _p(keys), _p(perm))
+    return keys, perm
+
+
+def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=None):
+    """One coupling pass (serial, id order) on copies of the state.  Returns the updated
+    (pos, vel, drag_old, active, force_fix, u_at)."""
+    lib = load()
+    _, pp = _params(cfg)
+    ppp = pcfg.to_c()
+    pos = np.ascontiguousarray(pos, np.float32).copy()
+    vel = np.ascontiguousarray(vel, np.float32).copy()
+    diam = np.ascontiguousarray(diam, np.float32)
+    drag_old = np.ascontiguousarray(drag_old, np.float32).copy()
+    active = np.ascontiguousarray(active, np.int32).copy()
+    u = np.ascontiguousarray(u, np.float32)
+    n = diam.shape[0]
+    if force_fix is None:
+        force_fix = np.zeros(3 * cfg.ncell, np.int64)
+    u_at = np.zeros((3, n), np.float32)
+    lib.orc_particles_couple(pp, ctypes.byref(ppp), _p(pos), _p(vel), _p(diam), _p(drag_old),
+                             _p(active), n, _p(u), _p(force_fix), _p(u_at))
+    return pos, vel, drag_old, active, force_fix, u_at
+
+
+def adjoint_step(cfg, flags, f_t, lam_next, eps=None, grad_eps=None, grad_inlet=None):
+    lib = load()
+    _, pp = _params(cfg)
+    lam_t = np.zeros_like(lam_next)
+    if eps is not None:
+        eps = np.ascontiguousarray(eps, np.float32)
+    lib.orc_adjoint_step_f64(pp, _p(flags), _p(np.ascontiguousarray(f_t, np.float64)),
+                             _p(np.ascontiguousarray(lam_next, np.float64)), _p(lam_t), _p(eps),
+                             _p(grad_eps), _p(grad_inlet))
+    return lam_t
+
+
+def outflow_loss(cfg, nsteps, flags=None, eps=None):
+    """J = sum over steps of the outflow flux, FP64 forward."""
+    red = np.zeros(6, np.float64)
+    run(cfg, nsteps, np.float64, flags=flags, eps=eps, reductions=red)
+    return float(red[4])
+
+
+def outflow_gradient(cfg, nsteps, flags=None, eps=None):
+    """Adjoint of outflow_loss by storing every state (small grids only)."""
+    if flags is None:
+        flags = build_flags(cfg)
+    f = init_equilibrium(cfg, flags, np.float64)
+    states = []
+    for _ in range(nsteps):
+        states.append(f)
+        f, _, _ = step(cfg, flags, f, eps=eps)
+    lam = np.zeros_like(f)
+    ge = np.zeros((cfg.nz, cfg.ny, cfg.nx), np.float64) if eps is not None else None
+    gi = np.zeros(16, np.float64)
+    for t in reversed(range(nsteps)):
+        lam = adjoint_step(cfg, flags, states[t], lam, eps=eps, grad_eps=ge, grad_inlet=gi)
+    return ge, gi

@@ -1,0 +1,693 @@
+// pog_oracle.cpp -- CPU restatement of the reference hot path.  TEST INFRASTRUCTURE ONLY.
+//
+// This file is the oracle the CUDA library (libpog.so) is checked against.  Only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg load it, and only as the checker
+// or the timed CPU baseline; the product never calls it.
+//
+// The reference (latteine1217/pour-over-coffee-lbm) is Python + Taichi and cannot run here
+// (no Taichi).  Each function below restates the reference code it cites, with the
+// reference's own structure (separate macroscopic pass, collide, push streaming into a
+// second buffer with half-way bounce-back), written as plain loops in FP32 or FP64.  Where the
+// reference contradicts itself the build spec decides (D3Q19 ordering of config/core.py,
+// standard Guo forcing, lattice-unit Stokes drag); those choices are the same ones the CUDA
+// library makes, and they are listed in the project's design notes.
+//
+// Pinning: the equilibrium, moment, trilinear-interpolation, LES-gate, Forchheimer and
+// under-relaxation functions are checked against the known-answer cases of the reference's
+// own tests (tests/test_lbm_algorithms.py, test_trilinear_interpolation.py,
+// test_les_turbulence.py, test_forchheimer.py, test_filter_paper.py,
+// test_under_relaxation.py) in tests/test_oracle_kat.py.  No reference test pins a
+// multi-step trajectory, so trajectory parity is pinned by this restatement only.
+//
+// Build: g++ -O2 -fopenmp -ffp-contract=off -shared -fPIC (see oracle/build.py).  No FP
+// contraction, so particle arithmetic is bit-identical with the GPU kernels (which are also
+// compiled without contraction).
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "../include/pog.h"
+
+namespace {
+
+// D3Q19 in the reference's config/core.py:36-47 ordering.
+const int CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0};
+const int CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1};
+const double WD[19] = {1.0 / 3.0,  1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0, 1.0 / 18.0,
+                       1.0 / 18.0, 1.0 / 18.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                       1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0,
+                       1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
+
+// opposite(q): the search of legacy/lbm_solver.py:431-439 over the table above.
+int OPP[19];
+struct OppInit {
+  OppInit() {
+    for (int q = 0; q < 19; ++q)
+      for (int p = 0; p < 19; ++p)
+        if (CX[q] == -CX[p] && CY[q] == -CY[p] && CZ[q] == -CZ[p]) OPP[q] = p;
+  }
+} opp_init;
+
+template <typename T>
+T wq(int q) {
+  return (T)WD[q];
+}
+
+// Storage rounding of the shifted forms (f - w*rho0): FP16 is scaled by 2^12 so small
+// deviations stay normal numbers; BF16 needs no scale.
+const float F16_SCALE = 4096.0f;
+
+float round_bf16(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;  // inf/nan unchanged
+  uint32_t lsb = (u >> 16) & 1u;
+  u += 0x7fffu + lsb;
+  u &= 0xffff0000u;
+  float y;
+  memcpy(&y, &u, 4);
+  return y;
+}
+float round_f16s(float x) {
+  _Float16 h = (_Float16)(x * F16_SCALE);
+  return (float)h / F16_SCALE;
+}
+
+template <typename T>
+T store_round(int storage, T v, int q, T rho0) {
+  if (storage == POG_STORE_F16S) {
+    T w = wq<T>(q) * rho0;
+    return w + (T)round_f16s((float)(v - w));
+  }
+  if (storage == POG_STORE_BF16S) {
+    T w = wq<T>(q) * rho0;
+    return w + (T)round_bf16((float)(v - w));
+  }
+  return v;
+}
+
+struct Geo {
+  int nx, ny, nz;
+  long long n;
+  double cx, cy, tanth;
+  long long idx(int i, int j, int k) const { return ((long long)k * ny + j) * nx + i; }
+};
+
+Geo make_geo(const pog_params* p) {
+  Geo g;
+  g.nx = p->nx;
+  g.ny = p->ny;
+  g.nz = p->nz;
+  g.n = (long long)p->nx * p->ny * p->nz;
+  g.cx = p->center_x < 0 ? 0.5 * p->nx : (double)p->center_x;
+  g.cy = p->center_y < 0 ? 0.5 * p->ny : (double)p->center_y;
+  g.tanth = tan((double)p->cone_half_angle_deg * M_PI / 180.0);
+  return g;
+}
+
+// ---------------------------------------------------------------------------------------
+// Equilibrium: lbm_algorithms.py:183-218, f_eq = w rho (1 + 3 e.u + 4.5 (e.u)^2 - 1.5 u.u)
+template <typename T>
+void equilibrium(T rho, T ux, T uy, T uz, T feq[19]) {
+  T usq = ux * ux + uy * uy + uz * uz;
+  for (int q = 0; q < 19; ++q) {
+    T eu = (T)CX[q] * ux + (T)CY[q] * uy + (T)CZ[q] * uz;
+    feq[q] = wq<T>(q) * rho * ((T)1 + (T)3 * eu + (T)4.5 * eu * eu - (T)1.5 * usq);
+  }
+}
+
+// Radial inlet profile u_z(r) = u_inlet (1 + sum_k a_k T_k(2r/R - 1)), Chebyshev T_k.
+// `coef` overrides p->inlet_coef (the adjoint oracle passes dual numbers there).
+template <typename T>
+T inlet_velocity(const pog_params* p, T r, const T* coef = nullptr) {
+  T a[POG_INLET_NCOEF];
+  for (int k = 0; k < POG_INLET_NCOEF; ++k) a[k] = coef ? coef[k] : (T)p->inlet_coef[k];
+  T R = (T)p->inlet_radius;
+  T s = R > (T)0 ? (T)2 * r / R - (T)1 : (T)0;
+  T t0 = (T)1, t1 = s, acc = a[0];
+  acc += a[1] * t1;
+  for (int k = 2; k < POG_INLET_NCOEF; ++k) {
+    T t2 = (T)2 * s * t1 - t0;
+    acc += a[k] * t2;
+    t0 = t1;
+    t1 = t2;
+  }
+  return (T)p->u_inlet * ((T)1 + acc);
+}
+
+// Kozeny-Carman permeability and Ergun-type Forchheimer coefficient at porosity eps,
+// normalised so that (permeability, forchheimer) are the values at p->porosity
+// (filter_paper.py:423-469 uses K = d^2 eps^3/(180(1-eps)^2), beta = 1.75(1-eps)/eps^3).
+template <typename T>
+void porous_coeffs(const pog_params* p, T eps, T& K, T& CF) {
+  T e0 = (T)p->porosity;
+  T g0 = e0 * e0 * e0 / (((T)1 - e0) * ((T)1 - e0));
+  T g = eps * eps * eps / (((T)1 - eps) * ((T)1 - eps));
+  K = (T)p->permeability * (g / g0);
+  T r = e0 / eps;
+  CF = (T)p->forchheimer * (r * sqrt(r));
+}
+
+// LES nu_sgs from central differences of a stored velocity field
+// (les_turbulence.py:318-380).  u is [3][n].  Returns 0 where the reference does.
+template <typename T>
+T les_nu_stencil(const pog_params* p, const Geo& g, const uint8_t* flags, const T* u, int i,
+                 int j, int k) {
+  if (i < 1 || j < 1 || k < 1 || i > g.nx - 2 || j > g.ny - 2 || k > g.nz - 2) return 0;
+  long long c = g.idx(i, j, k);
+  if (flags[c] & POG_CELL_POROUS) return 0;  // filter zone: LES mask 0 (filter_paper.py:199)
+  const T* ux = u;
+  const T* uy = u + g.n;
+  const T* uz = u + 2 * g.n;
+  long long ip = g.idx(i + 1, j, k), im = g.idx(i - 1, j, k);
+  long long jp = g.idx(i, j + 1, k), jm = g.idx(i, j - 1, k);
+  long long kp = g.idx(i, j, k + 1), km = g.idx(i, j, k - 1);
+  T dudx = (ux[ip] - ux[im]) * (T)0.5, dudy = (ux[jp] - ux[jm]) * (T)0.5,
+    dudz = (ux[kp] - ux[km]) * (T)0.5;
+  T dvdx = (uy[ip] - uy[im]) * (T)0.5, dvdy = (uy[jp] - uy[jm]) * (T)0.5,
+    dvdz = (uy[kp] - uy[km]) * (T)0.5;
+  T dwdx = (uz[ip] - uz[im]) * (T)0.5, dwdy = (uz[jp] - uz[jm]) * (T)0.5,
+    dwdz = (uz[kp] - uz[km]) * (T)0.5;
+  T S11 = dudx, S22 = dvdy, S33 = dwdz;
+  T S12 = (T)0.5 * (dudy + dvdx), S13 = (T)0.5 * (dudz + dwdx), S23 = (T)0.5 * (dvdz + dwdy);
+  T smag = sqrt((T)2 * (S11 * S11 + S22 * S22 + S33 * S33 +
+                        (T)2 * (S12 * S12 + S13 * S13 + S23 * S23)));
+  if (smag < (T)p->les_strain_floor) return 0;
+  T cs = (T)p->cs_smag;
+  T nu = cs * cs * smag;
+  return std::min(nu, (T)p->les_nu_max);
+}
+
+// Per-cell collision (legacy/lbm_solver.py:488-535 moments, :537-579 BGK, :594-607/688-764
+// forcing, filter_paper.py:471-536 porous drag, boundary_conditions.py:384-409 inlet/outlet).
+// Inputs: incoming populations f, flag, optional external force Fe and porosity.  Output:
+// post-collision populations fs, rho, u, and reduction contributions.
+template <typename T>
+void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int k, const T f[19],
+             const T* Fe, bool has_eps, T eps, T nu_stencil, T fs[19], T& rho_o, T u_o[3],
+             double* red, const T* coef = nullptr) {
+  T rho = 0, mx = 0, my = 0, mz = 0;
+  for (int q = 0; q < 19; ++q) {
+    rho += f[q];
+    mx += (T)CX[q] * f[q];
+    my += (T)CY[q] * f[q];
+    mz += (T)CZ[q] * f[q];
+  }
+  T ux, uy, uz;
+  T feq[19];
+  if (flag & POG_CELL_INLET) {
+    T dx = (T)i - (T)g.cx, dy = (T)j - (T)g.cy;
+    T r = sqrt(dx * dx + dy * dy);
+    ux = 0;
+    uy = 0;
+    uz = inlet_velocity<T>(p, r, coef);
+    equilibrium<T>(rho, ux, uy, uz, fs);
+  } else if (flag & POG_CELL_OUTLET) {
+    ux = mx / rho;
+    uy = my / rho;
+    uz = mz / rho;
+    equilibrium<T>((T)p->rho_outlet, ux, uy, uz, fs);
+    if (red) red[POG_RED_OUTFLOW] += -(double)mz;
+  } else {
+    T Gx = rho * (T)p->gx, Gy = rho * (T)p->gy, Gz = rho * (T)p->gz;
+    if (Fe) {
+      Gx += Fe[0];
+      Gy += Fe[1];
+      Gz += Fe[2];
+    }
+    T vx = (mx + (T)0.5 * Gx) / rho, vy = (my + (T)0.5 * Gy) / rho, vz = (mz + (T)0.5 * Gz) / rho;
+    T Fx = Gx, Fy = Gy, Fz = Gz;
+    ux = vx;
+    uy = vy;
+    uz = vz;
+    bool porous = (flag & POG_CELL_POROUS) != 0;
+    T nu0 = ((T)p->tau - (T)0.5) / (T)3;
+    if (porous) {
+      T K, CF;
+      if (has_eps) {
+        porous_coeffs<T>(p, eps, K, CF);
+      } else {
+        K = (T)p->permeability;
+        CF = (T)p->forchheimer;
+      }
+      T sK = sqrt(K);
+      if (p->drag_mode == POG_DRAG_SEMI_IMPLICIT) {
+        T c0 = (T)0.5 * ((T)1 + (T)0.5 * nu0 / K);
+        T c1 = (T)0.5 * CF / sK;
+        T vm = sqrt(vx * vx + vy * vy + vz * vz);
+        T s = (T)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
+        ux = vx * s;
+        uy = vy * s;
+        uz = vz * s;
+        T um = sqrt(ux * ux + uy * uy + uz * uz);
+        T coef = rho * (nu0 / K + CF / sK * um);
+        Fx = Gx - coef * ux;
+        Fy = Gy - coef * uy;
+        Fz = Gz - coef * uz;
+      } else {
+        T vm = sqrt(vx * vx + vy * vy + vz * vz);
+        T coef = rho * (nu0 / K + CF / sK * vm);
+        T dx = -coef * vx, dy = -coef * vy, dz = -coef * vz;
+        T dm = sqrt(dx * dx + dy * dy + dz * dz);
+        T cap = (T)p->drag_cap;
+        if (dm > cap) {
+          T sc = cap / dm;
+          dx *= sc;
+          dy *= sc;
+          dz *= sc;
+        }
+        Fx = Gx + dx;
+        Fy = Gy + dy;
+        Fz = Gz + dz;
+        ux = (mx + (T)0.5 * Fx) / rho;
+        uy = (my + (T)0.5 * Fy) / rho;
+        uz = (mz + (T)0.5 * Fz) / rho;
+      }
+    }
+    equilibrium<T>(rho, ux, uy, uz, feq);
+    T tau0 = (T)p->tau;
+    T nu = 0;
+    if (!porous && p->les_mode == POG_LES_LOCAL) {
+      T P[6] = {0, 0, 0, 0, 0, 0};  // xx yy zz xy xz yz
+      for (int q = 0; q < 19; ++q) {
+        T d = f[q] - feq[q];
+        T ex = (T)CX[q], ey = (T)CY[q], ez = (T)CZ[q];
+        P[0] += ex * ex * d;
+        P[1] += ey * ey * d;
+        P[2] += ez * ez * d;
+        P[3] += ex * ey * d;
+        P[4] += ex * ez * d;
+        P[5] += ey * ez * d;
+      }
+      T PP = P[0] * P[0] + P[1] * P[1] + P[2] * P[2] + (T)2 * (P[3] * P[3] + P[4] * P[4] + P[5] * P[5]);
+      T Q = sqrt((T)2 * PP);
+      T cs = (T)p->cs_smag;
+      T tl = (T)0.5 * (tau0 + sqrt(tau0 * tau0 + (T)18 * cs * cs * Q / rho));
+      T smag = (T)3 * Q / ((T)2 * rho * tl);
+      nu = (tl - tau0) / (T)3;
+      if (smag < (T)p->les_strain_floor) nu = 0;
+      nu = std::min(nu, (T)p->les_nu_max);
+    } else if (!porous && p->les_mode == POG_LES_STENCIL) {
+      nu = nu_stencil;
+    }
+    T tau = tau0 + (T)3 * nu;
+    if (p->clamp_tau) tau = std::max((T)p->tau_min, std::min((T)p->tau_max, tau));
+    T omega = (T)1 / tau;
+    if (p->forcing_mode == POG_FORCING_GUO) {
+      T pref = (T)1 - (T)0.5 * omega;
+      for (int q = 0; q < 19; ++q) {
+        T ex = (T)CX[q], ey = (T)CY[q], ez = (T)CZ[q];
+        T eu = ex * ux + ey * uy + ez * uz;
+        T eF = ex * Fx + ey * Fy + ez * Fz;
+        T emuF = (ex - ux) * Fx + (ey - uy) * Fy + (ez - uz) * Fz;
+        T S = pref * wq<T>(q) * ((T)3 * emuF + (T)9 * eu * eF);
+        fs[q] = f[q] - omega * (f[q] - feq[q]) + S;
+      }
+    } else {
+      // legacy/lbm_solver.py:594-607 and 688-764
+      T taus = std::max((T)0.6, std::min((T)1.5, tau));
+      T fn = sqrt(Fx * Fx + Fy * Fy + Fz * Fz);
+      T sf = fn > (T)10 ? (T)10 / fn : (T)1;
+      T fx = Fx * sf, fy = Fy * sf, fz = Fz * sf;
+      T un = sqrt(ux * ux + uy * uy + uz * uz);
+      T su = un <= (T)0.2 ? (T)1 : (T)0.2 / un;
+      T sx = ux * su, sy = uy * su, sz = uz * su;
+      T uf = sx * fx + sy * fy + sz * fz;
+      for (int q = 0; q < 19; ++q) {
+        T S = 0;
+        if (fn > (T)1e-15) {
+          T ex = (T)CX[q], ey = (T)CY[q], ez = (T)CZ[q];
+          T eu = ex * sx + ey * sy + ez * sz;
+          T ef = ex * fx + ey * fy + ez * fz;
+          S = wq<T>(q) * ((T)1 - (T)0.5 / taus) * ((T)3 * ef + (T)9 * eu * uf);
+          S = std::max((T)-0.5, std::min((T)0.5, S));
+        }
+        fs[q] = f[q] - omega * (f[q] - feq[q]) + S;
+      }
+    }
+  }
+  rho_o = rho;
+  u_o[0] = ux;
+  u_o[1] = uy;
+  u_o[2] = uz;
+  if (red) {
+    red[POG_RED_MASS] += (double)rho;
+    red[POG_RED_MOMX] += (double)rho * (double)ux;
+    red[POG_RED_MOMY] += (double)rho * (double)uy;
+    red[POG_RED_MOMZ] += (double)rho * (double)uz;
+    if (!std::isfinite((double)rho) || !std::isfinite((double)ux) || !std::isfinite((double)uy) ||
+        !std::isfinite((double)uz))
+      red[POG_RED_NONFINITE] += 1.0;
+  }
+}
+
+// One push step on natural layout (legacy/lbm_solver.py:460-486 + :609-628): every fluid
+// cell collides and pushes f*_q to x+e_q, or into opp(q) at x when x+e_q is solid.
+template <typename T>
+int step_push(const pog_params* p, const uint8_t* flags, const T* f, T* fo, const float* Fe,
+              const float* eps, const T* u_prev, T* rho_out, T* u_out, double* red) {
+  Geo g = make_geo(p);
+  const long long n = g.n;
+  double acc[POG_RED_COUNT] = {0, 0, 0, 0, 0, 0};
+  const T rho0 = (T)p->rho0;
+#pragma omp parallel
+  {
+    double loc[POG_RED_COUNT] = {0, 0, 0, 0, 0, 0};
+#pragma omp for schedule(static)
+    for (int k = 0; k < g.nz; ++k)
+      for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i) {
+          long long c = g.idx(i, j, k);
+          uint8_t fl = flags[c];
+          if (fl & POG_CELL_SOLID) continue;
+          T fin[19], fs[19], rho, u[3];
+          for (int q = 0; q < 19; ++q) fin[q] = f[q * n + c];
+          T fe[3];
+          const T* fep = nullptr;
+          if (Fe) {
+            fe[0] = (T)Fe[c];
+            fe[1] = (T)Fe[n + c];
+            fe[2] = (T)Fe[2 * n + c];
+            fep = fe;
+          }
+          T nus = 0;
+          if (p->les_mode == POG_LES_STENCIL && u_prev)
+            nus = les_nu_stencil<T>(p, g, flags, u_prev, i, j, k);
+          collide<T>(p, g, fl, i, j, k, fin, fep, eps != nullptr, eps ? (T)eps[c] : (T)0, nus, fs,
+                     rho, u, red ? loc : nullptr);
+          if (rho_out) rho_out[c] = rho;
+          if (u_out) {
+            u_out[c] = u[0];
+            u_out[n + c] = u[1];
+            u_out[2 * n + c] = u[2];
+          }
+          for (int q = 0; q < 19; ++q) {
+            long long nb = g.idx(i + CX[q], j + CY[q], k + CZ[q]);
+            T v = store_round<T>(p->storage, fs[q], q, rho0);
+            if (flags[nb] & POG_CELL_SOLID)
+              fo[OPP[q] * n + c] = v;
+            else
+              fo[q * n + nb] = v;
+          }
+        }
+#pragma omp critical
+    for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] += loc[r];
+  }
+  if (red)
+    for (int r = 0; r < POG_RED_COUNT; ++r) red[r] += acc[r];
+  return 0;
+}
+
+template <typename T>
+void init_eq(const pog_params* p, const uint8_t* flags, T* f, T rho0, T ux, T uy, T uz) {
+  Geo g = make_geo(p);
+  T feq[19];
+  equilibrium<T>(rho0, ux, uy, uz, feq);
+  for (int q = 0; q < 19; ++q) feq[q] = store_round<T>(p->storage, feq[q], q, (T)p->rho0);
+  for (long long c = 0; c < g.n; ++c)
+    for (int q = 0; q < 19; ++q) f[q * g.n + c] = (flags[c] & POG_CELL_SOLID) ? (T)0 : feq[q];
+}
+
+}  // namespace
+
+// =========================================================================================
+extern "C" {
+
+int orc_d3q19_tables(int* cx, int* cy, int* cz, int* opp, double* w) {
+  for (int q = 0; q < 19; ++q) {
+    cx[q] = CX[q];
+    cy[q] = CY[q];
+    cz[q] = CZ[q];
+    opp[q] = OPP[q];
+    w[q] = WD[q];
+  }
+  return 0;
+}
+
+// V60 geometry + band + inlet/outlet (filter_paper.py:206-364).  FP64, no contraction.
+// solid: the outer one-cell shell; below the apex everything outside the drain hole; above it
+// the cone wall (rc, rc + wall] minus the hole bore.  Inlet disk on k = nz-2, outlet disk on
+// k = 1.  Porous band: fluid cells at/above the apex inside the wall within band_thickness of
+// it (this includes the hole bore, which the filter paper covers).
+int orc_build_flags(const pog_params* p, uint8_t* flags) {
+  if (p->inlet_control) return -1;  // device pointer: not readable by the CPU restatement
+  Geo g = make_geo(p);
+  const double apex = p->cone_apex_z, wall = p->cone_wall, hole = p->hole_radius;
+  const double rin = p->inlet_radius, band = p->band_thickness;
+  std::vector<uint8_t> solid(g.n);
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) {
+        double x = i, y = j, z = k;
+        double dx = x - g.cx, dy = y - g.cy;
+        double r = sqrt(dx * dx + dy * dy);
+        bool s = (i == 0 || j == 0 || k == 0 || i == g.nx - 1 || j == g.ny - 1 || k == g.nz - 1);
+        double rc = (z - apex) * g.tanth;
+        if (z < apex) {
+          if (r > hole) s = true;
+        } else if (r > rc && r <= rc + wall && r > hole) {
+          s = true;
+        }
+        solid[g.idx(i, j, k)] = s ? 1 : 0;
+      }
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) {
+        long long c = g.idx(i, j, k);
+        uint8_t fl = 0;
+        if (solid[c]) {
+          flags[c] = POG_CELL_SOLID;
+          continue;
+        }
+        double x = i, y = j, z = k;
+        double dx = x - g.cx, dy = y - g.cy;
+        double r = sqrt(dx * dx + dy * dy);
+        double rc = (z - apex) * g.tanth;
+        if (k == g.nz - 2 && r <= rin) fl |= POG_CELL_INLET;
+        if (k == 1 && r <= hole) fl |= POG_CELL_OUTLET;
+        if (!(fl & (POG_CELL_INLET | POG_CELL_OUTLET)) && band > 0 && z >= apex && r > rc - band &&
+            r <= rc + wall)
+          fl |= POG_CELL_POROUS;
+        for (int q = 1; q < 19; ++q)
+          if (solid[g.idx(i + CX[q], j + CY[q], k + CZ[q])]) fl |= POG_CELL_NEAR_SOLID;
+        flags[c] = fl;
+      }
+  return 0;
+}
+
+int orc_init_equilibrium_f32(const pog_params* p, const uint8_t* flags, float* f, float rho0,
+                             float ux, float uy, float uz) {
+  init_eq<float>(p, flags, f, rho0, ux, uy, uz);
+  return 0;
+}
+int orc_init_equilibrium_f64(const pog_params* p, const uint8_t* flags, double* f, double rho0,
+                             double ux, double uy, double uz) {
+  init_eq<double>(p, flags, f, rho0, ux, uy, uz);
+  return 0;
+}
+
+// One step, natural layout, f_out must be a different buffer.  u_prev: [3][n] velocity of the
+// previous step (LES stencil mode) or null.  Fe: [3][n] float external force or null.
+int orc_step_f32(const pog_params* p, const uint8_t* flags, const float* f, float* fo,
+                 const float* Fe, const float* eps, const float* u_prev, float* rho_out,
+                 float* u_out, double* red) {
+  return step_push<float>(p, flags, f, fo, Fe, eps, u_prev, rho_out, u_out, red);
+}
+int orc_step_f64(const pog_params* p, const uint8_t* flags, const double* f, double* fo,
+                 const float* Fe, const float* eps, const double* u_prev, double* rho_out,
+                 double* u_out, double* red) {
+  return step_push<double>(p, flags, f, fo, Fe, eps, u_prev, rho_out, u_out, red);
+}
+
+// ---- function-level helpers for the known-answer tests ------------------------------------
+void orc_equilibrium_f64(double rho, double ux, double uy, double uz, double* feq) {
+  equilibrium<double>(rho, ux, uy, uz, feq);
+}
+void orc_equilibrium_f32(float rho, float ux, float uy, float uz, float* feq) {
+  equilibrium<float>(rho, ux, uy, uz, feq);
+}
+// rho = sum f, u = sum f e / rho (lbm_algorithms.py macroscopic_density/velocity_unified).
+void orc_moments_f64(const double* f, double* rho, double* u) {
+  double r = 0, mx = 0, my = 0, mz = 0;
+  for (int q = 0; q < 19; ++q) {
+    r += f[q];
+    mx += CX[q] * f[q];
+    my += CY[q] * f[q];
+    mz += CZ[q] * f[q];
+  }
+  *rho = r;
+  u[0] = r > 1e-12 ? mx / r : 0;
+  u[1] = r > 1e-12 ? my / r : 0;
+  u[2] = r > 1e-12 ? mz / r : 0;
+}
+// LES nu_sgs field from a [3][n] velocity (les_turbulence.py:318-380).
+int orc_les_nu_f32(const pog_params* p, const uint8_t* flags, const float* u, float* nu) {
+  Geo g = make_geo(p);
+  for (int k = 0; k < g.nz; ++k)
+    for (int j = 0; j < g.ny; ++j)
+      for (int i = 0; i < g.nx; ++i) nu[g.idx(i, j, k)] = les_nu_stencil<float>(p, g, flags, u, i, j, k);
+  return 0;
+}
+// Darcy-Forchheimer force density at a given rho/u in porous cells, the drag_mode form
+// (filter_paper.py:471-536).  F: [3][n]; zero outside the band.
+int orc_porous_force_f32(const pog_params* p, const uint8_t* flags, const float* rho,
+                         const float* u, float* F) {
+  Geo g = make_geo(p);
+  const long long n = g.n;
+  float nu0 = (p->tau - 0.5f) / 3.0f;
+  for (long long c = 0; c < n; ++c) {
+    F[c] = F[n + c] = F[2 * n + c] = 0;
+    if (!(flags[c] & POG_CELL_POROUS) || (flags[c] & POG_CELL_SOLID)) continue;
+    float K = p->permeability, CF = p->forchheimer, sK = sqrtf(K);
+    float ux = u[c], uy = u[n + c], uz = u[2 * n + c];
+    float um = sqrtf(ux * ux + uy * uy + uz * uz);
+    float coef = rho[c] * (nu0 / K + CF / sK * um);
+    float dx = -coef * ux, dy = -coef * uy, dz = -coef * uz;
+    if (p->drag_mode == POG_DRAG_EXPLICIT_CAP) {
+      float dm = sqrtf(dx * dx + dy * dy + dz * dz);
+      if (dm > p->drag_cap) {
+        float s = p->drag_cap / dm;
+        dx *= s;
+        dy *= s;
+        dz *= s;
+      }
+    }
+    F[c] = dx;
+    F[n + c] = dy;
+    F[2 * n + c] = dz;
+  }
+  return 0;
+}
+void orc_inlet_velocity_f64(const pog_params* p, const double* r, double* uz, int m) {
+  for (int i = 0; i < m; ++i) uz[i] = inlet_velocity<double>(p, r[i]);
+}
+float orc_round_storage(int storage, float v, int q, float rho0) {
+  return store_round<float>(storage, v, q, rho0);
+}
+
+}  // extern "C"
+
+// =========================================================================================
+// Adjoint oracle: forward-mode dual numbers pushed through the same collide<T> above.  For a
+// fluid cell the 19 incoming populations, the cell porosity and the 16 inlet coefficients
+// are seeded as independent directions, which gives the exact Jacobian of the restated
+// collision; the adjoint of one push step is then lam_t(c) = J^T lam*(c) (+ dflux/df), with
+// lam* pulled through the transpose of push streaming.  This is automatic differentiation of
+// the restatement, independent of the hand-derived CUDA adjoint it checks.
+namespace {
+const int ND = 19 + 1 + POG_INLET_NCOEF;  // f_q, eps, a_k
+struct Dual {
+  double v;
+  double d[ND];
+  Dual() : v(0) { memset(d, 0, sizeof(d)); }
+  Dual(double x) : v(x) { memset(d, 0, sizeof(d)); }  // NOLINT (implicit from constants)
+  explicit operator double() const { return v; }
+};
+inline Dual operator+(const Dual& a, const Dual& b) {
+  Dual r(a.v + b.v);
+  for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+inline Dual operator-(const Dual& a, const Dual& b) {
+  Dual r(a.v - b.v);
+  for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+inline Dual operator-(const Dual& a) {
+  Dual r(-a.v);
+  for (int i = 0; i < ND; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+inline Dual operator*(const Dual& a, const Dual& b) {
+  Dual r(a.v * b.v);
+  for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+inline Dual operator/(const Dual& a, const Dual& b) {
+  Dual r(a.v / b.v);
+  for (int i = 0; i < ND; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) / (b.v * b.v);
+  return r;
+}
+inline Dual& operator+=(Dual& a, const Dual& b) { return a = a + b; }
+inline Dual& operator-=(Dual& a, const Dual& b) { return a = a - b; }
+inline Dual& operator*=(Dual& a, const Dual& b) { return a = a * b; }
+inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+inline Dual sqrt(const Dual& a) {
+  Dual r(::sqrt(a.v));
+  double g = a.v > 0 ? 0.5 / r.v : 0.0;  // zero subgradient at 0, as the CUDA adjoint
+  for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * g;
+  return r;
+}
+}  // namespace
+
+extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint8_t* flags, const double* ft,
+                                    const double* lam_next, double* lam_t, const float* eps,
+                                    double* grad_eps, double* grad_inlet) {
+  Geo g = make_geo(p);
+  const long long n = g.n;
+  std::vector<double> gi_acc(POG_INLET_NCOEF, 0.0);
+#pragma omp parallel
+  {
+    std::vector<double> gi(POG_INLET_NCOEF, 0.0);
+#pragma omp for schedule(static)
+    for (int k = 0; k < g.nz; ++k)
+      for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i) {
+          long long c = g.idx(i, j, k);
+          uint8_t fl = flags[c];
+          if (fl & POG_CELL_SOLID) {
+            for (int q = 0; q < 19; ++q) lam_t[q * n + c] = 0;
+            continue;
+          }
+          double ls[19];
+          for (int q = 0; q < 19; ++q) {
+            long long nb = g.idx(i + CX[q], j + CY[q], k + CZ[q]);
+            ls[q] = (flags[nb] & POG_CELL_SOLID) ? lam_next[OPP[q] * n + c] : lam_next[q * n + nb];
+          }
+          Dual f[19], fs[19], rho, u[3];
+          for (int q = 0; q < 19; ++q) {
+            f[q] = Dual(ft[q * n + c]);
+            f[q].d[q] = 1.0;
+          }
+          Dual e(eps ? (double)eps[c] : 0.0);
+          e.d[19] = 1.0;
+          Dual coef[POG_INLET_NCOEF];
+          for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) {
+            coef[kk] = Dual((double)p->inlet_coef[kk]);
+            coef[kk].d[20 + kk] = 1.0;
+          }
+          collide<Dual>(p, g, fl, i, j, k, f, nullptr, eps != nullptr, e, Dual(0.0), fs, rho, u,
+                        nullptr, coef);
+          for (int q = 0; q < 19; ++q) {
+            double acc = 0;
+            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[q];
+            if (fl & POG_CELL_OUTLET) acc += -(double)CZ[q];
+            lam_t[q * n + c] = acc;
+          }
+          if (grad_eps && eps) {
+            double acc = 0;
+            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[19];
+            grad_eps[c] += acc;
+          }
+          for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) {
+            double acc = 0;
+            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[20 + kk];
+            gi[kk] += acc;
+          }
+        }
+#pragma omp critical
+    for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) gi_acc[kk] += gi[kk];
+  }
+  if (grad_inlet)
+    for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) grad_inlet[kk] += gi_acc[kk];
+  return 0;
+}

@@ -1,0 +1,92 @@
+"""ctypes binding of libpog.so (the C ABI declared in include/pog.h).
+
+There is no CPU path: if the library cannot be built or loaded, every call raises.
+"""
+import ctypes
+import os
+import threading
+
+from . import build as _build
+from .params import PogParams, PogParticleParams
+
+_lock = threading.Lock()
+_lib = None
+
+POG_OK = 0
+ERRORS = {-1: "POG_E_ARG", -2: "POG_E_CUDA", -3: "POG_E_NAN", -4: "POG_E_INJECTED",
+          -5: "POG_E_RANGE", -6: "POG_E_STATE"}
+
+# (name, restype, argtypes) for every entry point of include/pog.h
+_P = ctypes.POINTER(PogParams)
+_PP = ctypes.POINTER(PogParticleParams)
+_v = ctypes.c_void_p
+_i = ctypes.c_int
+_ll = ctypes.c_longlong
+_f = ctypes.c_float
+SIGNATURES = [
+    ("pog_version", _i, []),
+    ("pog_last_error", ctypes.c_char_p, []),
+    ("pog_launch_count", _ll, [_i]),
+    ("pog_validate_params", _i, [_P]),
+    ("pog_build_flags", _i, [_P, _v, _v]),
+    ("pog_init_equilibrium", _i, [_P, _v, _v, _f, _f, _f, _f, _v]),
+    ("pog_step", _i, [_P, _v, _v, _ll, _i, _v, _v, _v, _v, _v, _v, _v, _v]),
+    ("pog_step_push", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
+    ("pog_export_natural", _i, [_P, _v, _v, _ll, _v, _i, _v]),
+    ("pog_import_natural", _i, [_P, _v, _i, _v, _v, _v]),
+    ("pog_macroscopic", _i, [_P, _v, _v, _ll, _v, _v, _v, _v]),
+    ("pog_particles_bin_scratch_bytes", ctypes.c_size_t, [_i]),
+    ("pog_particles_bin", _i, [_P, _v, _v, _i, _v, _v, _v, _v]),
+    ("pog_particles_couple", _i, [_P, _PP, _v, _v, _v, _v, _v, _i, _v, _v, _v, _v, _v, _v]),
+    ("pog_force_from_fixed", _i, [_P, _v, _v, _v]),
+    ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v]),
+]
+
+
+class PogError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "POG_E?"), code, msg))
+        self.code = code
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libpog.so (building it in-tree with nvcc when absent or stale)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing:
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError("libpog.so is missing; run pour_over_coffee_lbm_gb300.build.build()")
+        lib = ctypes.CDLL(_build.LIB)
+        for name, res, args in SIGNATURES:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(code: int):
+    if code != POG_OK:
+        msg = load().pog_last_error()
+        raise PogError(code, msg.decode() if msg else "")
+    return code
+
+
+def ptr(t):
+    """Device pointer of a tensor (or None -> NULL)."""
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_handle(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)

@@ -1,0 +1,396 @@
+// adjoint.cu -- reverse of one natural-layout step (pog_step_push), hand-derived.
+//
+// The reference has no adjoint (no Taichi autodiff on this path); this is new work checked
+// against central finite differences of the forward step and against the CPU restatement's
+// FP64 adjoint.  Forward step: f^{t+1} = Stream(Collide(f^t; eps, a)) with the per-cell
+// collision of collide.cuh.  Given lam^{t+1} = dJ/df^{t+1}, a cell x
+//   1. pulls lam*_q(x) = lam^{t+1}_q(x + e_q), or lam^{t+1}_{opp q}(x) when x + e_q is solid
+//      (the transpose of push streaming with half-way bounce-back, legacy/lbm_solver.py:
+//      609-628);
+//   2. recomputes its forward collision from f^t(x) and applies the transposed Jacobian
+//      (reverse mode by hand): f* = f_eq + (1 - w)(f - f_eq) + S(u, F, w), through the LES
+//      relaxation w = 1/tau(Pi_neq, rho) and the semi-implicit Darcy-Forchheimer velocity
+//      u = s(|v|, K(eps), C_F(eps)) v;
+//   3. adds dflux_t/df = -c_z on outlet cells (J = sum_t outflow flux);
+//   4. accumulates dJ/deps (per cell) and dJ/da_k (inlet profile) in FP64.
+// Supported forward configuration: LES off or LOCAL, drag SEMI_IMPLICIT, Guo forcing, no tau
+// clamp, no external force field.  Gated LES cells (|S| below the floor, nu at its cap) and
+// |u| = 0 points take the zero subgradient.
+#include "collide.cuh"
+
+namespace pog {
+
+constexpr int ADJ_BLOCK = 256;
+
+template <typename C>
+__device__ __forceinline__ void eq_all(C rho, C ux, C uy, C uz, C feq[19]) {
+  const C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
+#pragma unroll
+  for (int q = 0; q < 19; ++q) feq[q] = feq_q<C>(q, rho, ux, uy, uz, usq15);
+}
+
+// d(sum_q lam_q feq_q)/d(rho, u) for feq at (rho, u): returns bar_rho, bar_u.
+template <typename C>
+__device__ __forceinline__ void eq_vjp(const C lam[19], C rho, C ux, C uy, C uz, C& brho, C& bux,
+                                       C& buy, C& buz) {
+  C br = 0, bx = 0, by = 0, bz = 0;
+  const C usq = ux * ux + uy * uy + uz * uz;
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    const C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
+    const C wl = (C)wd(q) * lam[q];
+    br += wl * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - (C)1.5 * usq);
+    const C g = wl * rho * ((C)3 + (C)9 * eu);
+    bx += g * (C)cx(q) - wl * rho * (C)3 * ux;
+    by += g * (C)cy(q) - wl * rho * (C)3 * uy;
+    bz += g * (C)cz(q) - wl * rho * (C)3 * uz;
+  }
+  brho = br;
+  bux = bx;
+  buy = by;
+  buz = bz;
+}
+
+template <typename C>
+__device__ __forceinline__ C chebyshev_T(int k, C s) {
+  C t0 = (C)1, t1 = s;
+  if (k == 0) return t0;
+  for (int i = 2; i <= k; ++i) {
+    C t2 = (C)2 * s * t1 - t0;
+    t0 = t1;
+    t1 = t2;
+  }
+  return t1;
+}
+
+template <int S>
+__global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
+    const KParams kp, const typename Store<S>::E* __restrict__ ft,
+    const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
+    const uint8_t* __restrict__ flags, const float* __restrict__ eps,
+    double* __restrict__ grad_eps, double* __restrict__ grad_inlet) {
+  using St = Store<S>;
+  using C = typename St::C;
+  using E = typename St::E;
+  const uint32_t n = kp.n;
+  double ginl[POG_INLET_NCOEF];
+#pragma unroll
+  for (int k = 0; k < POG_INLET_NCOEF; ++k) ginl[k] = 0.0;
+  for (uint32_t c = blockIdx.x * ADJ_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_BLOCK) {
+    const uint8_t fl = flags[c];
+    if (fl & POG_CELL_SOLID) {
+#pragma unroll
+      for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)0;
+      continue;
+    }
+    // 1. transpose of push streaming
+    C ls[19];
+    const bool near = (fl & POG_CELL_NEAR_SOLID) != 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const uint32_t dst = c + (uint32_t)kp.off[q];
+      const bool wall = near && q != 0 && (flags[dst] & POG_CELL_SOLID);
+      ls[q] = wall ? (C)lam_next[(uint32_t)opp(q) * n + c] : (C)lam_next[(uint32_t)q * n + dst];
+    }
+    C f[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = (C)ft[(uint32_t)q * n + c];
+    C rho = 0, mx = 0, my = 0, mz = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      rho += f[q];
+      mx += (C)cx(q) * f[q];
+      my += (C)cy(q) * f[q];
+      mz += (C)cz(q) * f[q];
+    }
+    C brho = 0, bmx = 0, bmy = 0, bmz = 0;
+    C bf[19];
+    if (fl & POG_CELL_INLET) {
+      // f* = feq(rho, (0,0,uz(a)))
+      const C uz = inlet_uz<C>(kp, c);
+      C bux, buy, buz;
+      eq_vjp<C>(ls, rho, (C)0, (C)0, uz, brho, bux, buy, buz);
+      // uz = u_inlet (1 + sum a_k T_k(s))
+      uint32_t i = c % kp.nx, j = (c / kp.nx) % kp.ny;
+      C dx = (C)i - (C)kp.cxf, dy = (C)j - (C)kp.cyf;
+      C r = sqrt(dx * dx + dy * dy);
+      C R = (C)kp.inlet_R;
+      C s = R > (C)0 ? (C)2 * r / R - (C)1 : (C)0;
+      C t0 = (C)1, t1 = s;
+      const C ub = (C)(kp.inlet_ctl ? kp.inlet_ctl[0] : kp.u_inlet);
+      ginl[0] += (double)(buz * ub);
+      ginl[1] += (double)(buz * ub * t1);
+#pragma unroll
+      for (int k = 2; k < POG_INLET_NCOEF; ++k) {
+        C t2 = (C)2 * s * t1 - t0;
+        ginl[k] += (double)(buz * ub * t2);
+        t0 = t1;
+        t1 = t2;
+      }
+#pragma unroll
+      for (int q = 0; q < 19; ++q) bf[q] = brho;
+    } else if (fl & POG_CELL_OUTLET) {
+      const C ux = mx / rho, uy = my / rho, uz = mz / rho;
+      C br_out, bux, buy, buz;
+      eq_vjp<C>(ls, (C)kp.rho_out, ux, uy, uz, br_out, bux, buy, buz);
+      (void)br_out;
+      bmx = bux / rho;
+      bmy = buy / rho;
+      bmz = buz / rho;
+      brho = -(bux * ux + buy * uy + buz * uz) / rho;
+#pragma unroll
+      for (int q = 0; q < 19; ++q)
+        bf[q] = brho + (C)cx(q) * bmx + (C)cy(q) * bmy + (C)cz(q) * bmz - (C)cz(q);  // + dflux/df
+    } else {
+      // ---- forward recomputation ----
+      const C Gx = rho * (C)kp.gx, Gy = rho * (C)kp.gy, Gz = rho * (C)kp.gz;
+      const C vx = (mx + (C)0.5 * Gx) / rho, vy = (my + (C)0.5 * Gy) / rho, vz = (mz + (C)0.5 * Gz) / rho;
+      C ux = vx, uy = vy, uz = vz, Fx = Gx, Fy = Gy, Fz = Gz;
+      const bool porous = (fl & POG_CELL_POROUS) != 0;
+      C K = (C)kp.K0, CF = (C)kp.CF0, e = (C)kp.eps0;
+      C sK = 0, c0 = 0, c1 = 0, vm = 0, Ed = 0, D = 0, s = 0, um = 0, a = 0, b = 0, coef = 0;
+      const C nu0 = (C)kp.nu0;
+      if (porous) {
+        if (eps) {
+          e = (C)eps[c];
+          C g = e * e * e / (((C)1 - e) * ((C)1 - e));
+          K = (C)kp.K0 * (g / (C)kp.g0);
+          C rr = (C)kp.eps0 / e;
+          CF = (C)kp.CF0 * (rr * sqrt(rr));
+        }
+        sK = sqrt(K);
+        c0 = (C)0.5 * ((C)1 + (C)0.5 * nu0 / K);
+        c1 = (C)0.5 * CF / sK;
+        vm = sqrt(vx * vx + vy * vy + vz * vz);
+        Ed = sqrt(c0 * c0 + c1 * vm);
+        D = c0 + Ed;
+        s = (C)1 / D;
+        ux = vx * s;
+        uy = vy * s;
+        uz = vz * s;
+        um = sqrt(ux * ux + uy * uy + uz * uz);
+        a = nu0 / K;
+        b = CF / sK;
+        coef = rho * (a + b * um);
+        Fx = Gx - coef * ux;
+        Fy = Gy - coef * uy;
+        Fz = Gz - coef * uz;
+      }
+      C feq[19], neq[19];
+      eq_all<C>(rho, ux, uy, uz, feq);
+#pragma unroll
+      for (int q = 0; q < 19; ++q) neq[q] = f[q] - feq[q];
+      const C tau0 = (C)kp.tau;
+      C tau = tau0;
+      bool les_live = false;
+      C Pxx = 0, Pyy = 0, Pzz = 0, Pxy = 0, Pxz = 0, Pyz = 0, Q = 0, Rr = 0;
+      if (kp.les_mode == POG_LES_LOCAL && !porous) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+          const C d = neq[q];
+          Pxx += (C)(cx(q) * cx(q)) * d;
+          Pyy += (C)(cy(q) * cy(q)) * d;
+          Pzz += (C)(cz(q) * cz(q)) * d;
+          Pxy += (C)(cx(q) * cy(q)) * d;
+          Pxz += (C)(cx(q) * cz(q)) * d;
+          Pyz += (C)(cy(q) * cz(q)) * d;
+        }
+        const C PP = Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + (C)2 * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz);
+        Q = sqrt((C)2 * PP);
+        Rr = sqrt(tau0 * tau0 + (C)18 * (C)kp.cs2 * Q / rho);
+        const C tl = (C)0.5 * (tau0 + Rr);
+        const C smag = (C)3 * Q / ((C)2 * rho * tl);
+        C nu = (tl - tau0) / (C)3;
+        les_live = true;
+        if (smag < (C)kp.strain_floor) {
+          nu = 0;
+          les_live = false;
+        }
+        if (nu > (C)kp.nu_max) {
+          nu = (C)kp.nu_max;
+          les_live = false;
+        }
+        tau = tau0 + (C)3 * nu;
+      }
+      const C omega = (C)1 / tau;
+      const C A = (C)1 - (C)0.5 * omega;
+      const C uF = ux * Fx + uy * Fy + uz * Fz;
+      // ---- reverse ----
+      C bneq[19], bfeq[19];
+      C bomega = 0, bA = 0;
+      C bux = 0, buy = 0, buz = 0, bFx = 0, bFy = 0, bFz = 0;
+#pragma unroll
+      for (int q = 0; q < 19; ++q) {
+        const C lq = ls[q];
+        bfeq[q] = lq;
+        bneq[q] = ((C)1 - omega) * lq;
+        bomega -= lq * neq[q];
+        const C ex = (C)cx(q), ey = (C)cy(q), ez = (C)cz(q);
+        const C eu = ex * ux + ey * uy + ez * uz;
+        const C eF = ex * Fx + ey * Fy + ez * Fz;
+        const C Bq = (C)3 * (eF - uF) + (C)9 * eu * eF;
+        const C w = (C)wd(q);
+        bA += lq * w * Bq;
+        const C bB = lq * A * w;
+        bFx += bB * ((C)3 * (ex - ux) + (C)9 * eu * ex);
+        bFy += bB * ((C)3 * (ey - uy) + (C)9 * eu * ey);
+        bFz += bB * ((C)3 * (ez - uz) + (C)9 * eu * ez);
+        bux += bB * ((C)-3 * Fx + (C)9 * eF * ex);
+        buy += bB * ((C)-3 * Fy + (C)9 * eF * ey);
+        buz += bB * ((C)-3 * Fz + (C)9 * eF * ez);
+      }
+      bomega += (C)-0.5 * bA;
+      const C btau = -bomega / (tau * tau);
+      if (les_live) {
+        const C bnu = (C)3 * btau;
+        const C btl = bnu / (C)3;
+        const C bR = (C)0.5 * btl;
+        const C cs2 = (C)kp.cs2;
+        const C bQ = bR * (C)9 * cs2 / (rho * Rr);
+        brho += bR * (-(C)9 * cs2 * Q / (rho * rho * Rr));
+        const C bPP = Q > (C)0 ? bQ / Q : (C)0;
+        const C bPxx = (C)2 * Pxx * bPP, bPyy = (C)2 * Pyy * bPP, bPzz = (C)2 * Pzz * bPP;
+        const C bPxy = (C)4 * Pxy * bPP, bPxz = (C)4 * Pxz * bPP, bPyz = (C)4 * Pyz * bPP;
+#pragma unroll
+        for (int q = 0; q < 19; ++q)
+          bneq[q] += (C)(cx(q) * cx(q)) * bPxx + (C)(cy(q) * cy(q)) * bPyy + (C)(cz(q) * cz(q)) * bPzz +
+                     (C)(cx(q) * cy(q)) * bPxy + (C)(cx(q) * cz(q)) * bPxz + (C)(cy(q) * cz(q)) * bPyz;
+      }
+      // neq = f - feq
+#pragma unroll
+      for (int q = 0; q < 19; ++q) {
+        bf[q] = bneq[q];
+        bfeq[q] -= bneq[q];
+      }
+      // feq(rho, u)
+      {
+        C br, bx, by, bz;
+        eq_vjp<C>(bfeq, rho, ux, uy, uz, br, bx, by, bz);
+        brho += br;
+        bux += bx;
+        buy += by;
+        buz += bz;
+      }
+      C bvx, bvy, bvz, bGx, bGy, bGz;
+      if (porous) {
+        bGx = bFx;
+        bGy = bFy;
+        bGz = bFz;
+        const C bcoef = -(bFx * ux + bFy * uy + bFz * uz);
+        bux += -coef * bFx;
+        buy += -coef * bFy;
+        buz += -coef * bFz;
+        brho += bcoef * (a + b * um);
+        const C bum = bcoef * rho * b;
+        const C ba = bcoef * rho;
+        const C bb = bcoef * rho * um;
+        if (um > (C)0) {
+          bux += bum * ux / um;
+          buy += bum * uy / um;
+          buz += bum * uz / um;
+        }
+        const C bs = bux * vx + buy * vy + buz * vz;
+        bvx = s * bux;
+        bvy = s * buy;
+        bvz = s * buz;
+        const C bD = -bs / (D * D);
+        const C bc0 = bD * ((C)1 + c0 / Ed);
+        const C bc1 = bD * vm / ((C)2 * Ed);
+        const C bvm = bD * c1 / ((C)2 * Ed);
+        if (vm > (C)0) {
+          bvx += bvm * vx / vm;
+          bvy += bvm * vy / vm;
+          bvz += bvm * vz / vm;
+        }
+        if (eps && grad_eps) {
+          C bK = bc0 * (-(C)0.25 * nu0 / (K * K)) + bc1 * (-(C)0.25 * CF / (K * sK)) +
+                 ba * (-nu0 / (K * K)) + bb * (-(C)0.5 * CF / (K * sK));
+          C bCF = bc1 * (C)0.5 / sK + bb / sK;
+          C dK = K * ((C)3 / e + (C)2 / ((C)1 - e));
+          C dCF = (C)-1.5 * CF / e;
+          grad_eps[c] += (double)(bK * dK + bCF * dCF);
+        }
+      } else {
+        bvx = bux;
+        bvy = buy;
+        bvz = buz;
+        bGx = bFx;
+        bGy = bFy;
+        bGz = bFz;
+      }
+      // v = (m + G/2)/rho, G = rho g
+      bmx = bvx / rho;
+      bmy = bvy / rho;
+      bmz = bvz / rho;
+      bGx += (C)0.5 * bvx / rho;
+      bGy += (C)0.5 * bvy / rho;
+      bGz += (C)0.5 * bvz / rho;
+      brho += -(bvx * vx + bvy * vy + bvz * vz) / rho;
+      brho += bGx * (C)kp.gx + bGy * (C)kp.gy + bGz * (C)kp.gz;
+#pragma unroll
+      for (int q = 0; q < 19; ++q)
+        bf[q] += brho + (C)cx(q) * bmx + (C)cy(q) * bmy + (C)cz(q) * bmz;
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)bf[q];
+  }
+  if (grad_inlet) {
+    // block reduction of the 16 inlet-profile gradients (few cells contribute)
+    __shared__ double sm[POG_INLET_NCOEF][ADJ_BLOCK / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < POG_INLET_NCOEF; ++k) {
+      double x = ginl[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) sm[k][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < POG_INLET_NCOEF) {
+      double x = 0.0;
+      for (int w = 0; w < ADJ_BLOCK / 32; ++w) x += sm[threadIdx.x][w];
+      if (x != 0.0) atomicAdd(grad_inlet + threadIdx.x, x);
+    }
+  }
+}
+
+template <int S>
+static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* lt, const uint8_t* flags,
+                      const float* eps, double* ge, double* gi, cudaStream_t s) {
+  auto kern = adjoint_kernel<S>;
+  static thread_local int grid = 0;
+  if (grid == 0) grid = persistent_blocks((const void*)kern, ADJ_BLOCK);
+  if (grid <= 0) return set_error(POG_E_CUDA, "occupancy query failed");
+  int want = (int)((kp.n + ADJ_BLOCK - 1) / ADJ_BLOCK);
+  int g = want < grid ? want : grid;
+  using E = typename Store<S>::E;
+  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, ge, gi);
+  count_launch();
+  POG_TRY_CUDA(cudaGetLastError());
+  return POG_OK;
+}
+
+}  // namespace pog
+
+using namespace pog;
+
+extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next,
+                                void* lam_t, const uint8_t* flags, const float* porosity,
+                                double* grad_porosity, double* grad_inlet, void* stream) {
+  int rc = pog_validate_params(p);
+  if (rc) return rc;
+  if (!f_t || !lam_next || !lam_t || !flags) return set_error(POG_E_ARG, "NULL pointer");
+  if (lam_next == lam_t) return set_error(POG_E_ARG, "lam_next and lam_t must differ");
+  if (p->les_mode == POG_LES_STENCIL)
+    return set_error(POG_E_ARG, "adjoint supports les_mode OFF or LOCAL");
+  if (p->drag_mode != POG_DRAG_SEMI_IMPLICIT || p->forcing_mode != POG_FORCING_GUO || p->clamp_tau)
+    return set_error(POG_E_ARG, "adjoint supports semi-implicit drag, Guo forcing, no tau clamp");
+  if (grad_porosity && !porosity) return set_error(POG_E_ARG, "grad_porosity needs porosity");
+  KParams kp = make_kparams(p);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->storage == POG_STORE_F32)
+    return launch_adj<POG_STORE_F32>(kp, f_t, lam_next, lam_t, flags, porosity, grad_porosity, grad_inlet, s);
+  if (p->storage == POG_STORE_F64)
+    return launch_adj<POG_STORE_F64>(kp, f_t, lam_next, lam_t, flags, porosity, grad_porosity, grad_inlet, s);
+  return set_error(POG_E_ARG, "adjoint storage must be F32 or F64");
+}

@@ -1,0 +1,318 @@
+// collide.cuh -- per-cell physics shared by the AA kernel (lbm_aa.cu) and the push kernel
+// (lbm_push.cu): moments, inlet/outlet equilibrium overwrite, Guo forcing with gravity and the
+// external force, Darcy-Forchheimer drag in the filter band, LES relaxation, BGK collision.
+//
+// Reference structure restated (file:line in latteine1217/pour-over-coffee-lbm):
+//   moments + Guo half-force velocity   src/core/legacy/lbm_solver.py:488-535
+//   BGK + tau_eff = tau + 3 nu_sgs       src/core/legacy/lbm_solver.py:537-579
+//   equilibrium                          src/core/lbm_algorithms.py:183-218
+//   Guo forcing (standard form default)  docs/mathematical/mathematical_models.md:109-121,
+//                                        legacy form legacy/lbm_solver.py:594-607,688-764
+//   Smagorinsky nu_sgs + gates           src/physics/les_turbulence.py:318-380
+//   Darcy-Forchheimer drag               src/physics/filter_paper.py:471-536
+//   inlet/outlet overwrite               src/physics/boundary_conditions.py:194-324
+#pragma once
+#include "common.cuh"
+
+namespace pog {
+
+template <typename C>
+struct CellResult {
+  C rho, ux, uy, uz;
+  C outflow;  // -m_z on outlet cells, else 0
+};
+
+template <typename C>
+__device__ __forceinline__ C inlet_uz(const KParams& kp, uint32_t c) {
+  uint32_t i = c % kp.nx;
+  uint32_t j = (c / kp.nx) % kp.ny;
+  C dx = (C)i - (C)kp.cxf, dy = (C)j - (C)kp.cyf;
+  C r = sqrt(dx * dx + dy * dy);
+  C R = (C)kp.inlet_R;
+  C s = R > (C)0 ? (C)2 * r / R - (C)1 : (C)0;
+  const float* ctl = kp.inlet_ctl;
+  const float* a = ctl ? ctl + 1 : kp.coef;
+  C t0 = (C)1, t1 = s;
+  C acc = (C)a[0] + (C)a[1] * t1;
+#pragma unroll
+  for (int k = 2; k < POG_INLET_NCOEF; ++k) {
+    C t2 = (C)2 * s * t1 - t0;
+    acc += (C)a[k] * t2;
+    t0 = t1;
+    t1 = t2;
+  }
+  return (C)(ctl ? ctl[0] : kp.u_inlet) * ((C)1 + acc);
+}
+
+template <typename C>
+__device__ __forceinline__ C feq_q(int q, C rho, C ux, C uy, C uz, C usq15) {
+  C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
+  return (C)wd(q) * rho * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - usq15);
+}
+
+// f[19]: incoming populations on entry, post-collision populations on exit.
+// nu_st: nu_sgs from the velocity stencil (LES_STENCIL mode), computed by the caller.
+template <typename C>
+__device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t fl, uint32_t c,
+                                                      C f[19], const float* __restrict__ force,
+                                                      const float* __restrict__ eps, C nu_st) {
+  CellResult<C> res;
+  C rho = (C)0, mx = (C)0, my = (C)0, mz = (C)0;
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    rho += f[q];
+    if (cx(q) > 0) mx += f[q];
+    if (cx(q) < 0) mx -= f[q];
+    if (cy(q) > 0) my += f[q];
+    if (cy(q) < 0) my -= f[q];
+    if (cz(q) > 0) mz += f[q];
+    if (cz(q) < 0) mz -= f[q];
+  }
+  res.outflow = (C)0;
+  if (fl & (POG_CELL_INLET | POG_CELL_OUTLET)) {
+    C ux, uy, uz, rr;
+    if (fl & POG_CELL_INLET) {
+      ux = (C)0;
+      uy = (C)0;
+      uz = inlet_uz<C>(kp, c);
+      rr = rho;
+    } else {
+      ux = mx / rho;
+      uy = my / rho;
+      uz = mz / rho;
+      rr = (C)kp.rho_out;
+      res.outflow = -mz;
+    }
+    C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = feq_q<C>(q, rr, ux, uy, uz, usq15);
+    res.rho = rho;
+    res.ux = ux;
+    res.uy = uy;
+    res.uz = uz;
+    return res;
+  }
+
+  // Total non-drag force density: gravity rho*g plus the external (particle/plugin) force.
+  C Gx = rho * (C)kp.gx, Gy = rho * (C)kp.gy, Gz = rho * (C)kp.gz;
+  if (force) {
+    Gx += (C)force[c];
+    Gy += (C)force[kp.n + c];
+    Gz += (C)force[2u * kp.n + c];
+  }
+  C inv_rho = (C)1 / rho;
+  C ux = (mx + (C)0.5 * Gx) * inv_rho, uy = (my + (C)0.5 * Gy) * inv_rho,
+    uz = (mz + (C)0.5 * Gz) * inv_rho;
+  C Fx = Gx, Fy = Gy, Fz = Gz;
+  const bool porous = (fl & POG_CELL_POROUS) != 0;
+  if (porous) {
+    C K = (C)kp.K0, CF = (C)kp.CF0;
+    if (eps) {
+      C e = (C)eps[c];
+      C g = e * e * e / (((C)1 - e) * ((C)1 - e));
+      K = (C)kp.K0 * (g / (C)kp.g0);
+      C r = (C)kp.eps0 / e;
+      CF = (C)kp.CF0 * (r * sqrt(r));
+    }
+    C sK = sqrt(K);
+    C nu0 = (C)kp.nu0;
+    if (kp.drag_mode == POG_DRAG_SEMI_IMPLICIT) {
+      // Guo & Zhao 2002: u (1 + nu/(2K) + C_F|u|/(2 sqrt K)) = v, solved in closed form.
+      C c0 = (C)0.5 * ((C)1 + (C)0.5 * nu0 / K);
+      C c1 = (C)0.5 * CF / sK;
+      C vm = sqrt(ux * ux + uy * uy + uz * uz);
+      C s = (C)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
+      ux *= s;
+      uy *= s;
+      uz *= s;
+      C um = sqrt(ux * ux + uy * uy + uz * uz);
+      C coef = rho * (nu0 / K + CF / sK * um);
+      Fx = Gx - coef * ux;
+      Fy = Gy - coef * uy;
+      Fz = Gz - coef * uz;
+    } else {
+      C vm = sqrt(ux * ux + uy * uy + uz * uz);
+      C coef = rho * (nu0 / K + CF / sK * vm);
+      C dx = -coef * ux, dy = -coef * uy, dz = -coef * uz;
+      C dm = sqrt(dx * dx + dy * dy + dz * dz);
+      C cap = (C)kp.drag_cap;
+      if (dm > cap) {
+        C sc = cap / dm;
+        dx *= sc;
+        dy *= sc;
+        dz *= sc;
+      }
+      Fx = Gx + dx;
+      Fy = Gy + dy;
+      Fz = Gz + dz;
+      ux = (mx + (C)0.5 * Fx) * inv_rho;
+      uy = (my + (C)0.5 * Fy) * inv_rho;
+      uz = (mz + (C)0.5 * Fz) * inv_rho;
+    }
+  }
+  const C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
+  // f <- f - f_eq (non-equilibrium part), and the non-equilibrium stress for LES_LOCAL.
+  C Pxx = 0, Pyy = 0, Pzz = 0, Pxy = 0, Pxz = 0, Pyz = 0;
+  const bool les_local = kp.les_mode == POG_LES_LOCAL && !porous;
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    C d = f[q] - feq_q<C>(q, rho, ux, uy, uz, usq15);
+    f[q] = d;
+    if (les_local) {
+      if (cx(q) != 0) Pxx += d;
+      if (cy(q) != 0) Pyy += d;
+      if (cz(q) != 0) Pzz += d;
+      if (cx(q) * cy(q) > 0) Pxy += d;
+      if (cx(q) * cy(q) < 0) Pxy -= d;
+      if (cx(q) * cz(q) > 0) Pxz += d;
+      if (cx(q) * cz(q) < 0) Pxz -= d;
+      if (cy(q) * cz(q) > 0) Pyz += d;
+      if (cy(q) * cz(q) < 0) Pyz -= d;
+    }
+  }
+  const C tau0 = (C)kp.tau;
+  C nu = (C)0;
+  if (les_local) {
+    C PP = Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + (C)2 * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz);
+    C Q = sqrt((C)2 * PP);
+    C tl = (C)0.5 * (tau0 + sqrt(tau0 * tau0 + (C)18 * (C)kp.cs2 * Q * inv_rho));
+    C smag = (C)3 * Q / ((C)2 * rho * tl);
+    nu = (tl - tau0) / (C)3;
+    if (smag < (C)kp.strain_floor) nu = (C)0;
+    nu = nu < (C)kp.nu_max ? nu : (C)kp.nu_max;
+  } else if (kp.les_mode == POG_LES_STENCIL && !porous) {
+    nu = nu_st;
+  }
+  C tau = tau0 + (C)3 * nu;
+  if (kp.clamp_tau) tau = tau < (C)kp.tau_min ? (C)kp.tau_min : (tau > (C)kp.tau_max ? (C)kp.tau_max : tau);
+  const C omega = (C)1 / tau;
+  const C keep = (C)1 - omega;
+
+  if (kp.forcing_mode == POG_FORCING_GUO) {
+    const C pref = (C)1 - (C)0.5 * omega;
+    const C uF = ux * Fx + uy * Fy + uz * Fz;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
+      C eF = (C)cx(q) * Fx + (C)cy(q) * Fy + (C)cz(q) * Fz;
+      C S = pref * (C)wd(q) * ((C)3 * (eF - uF) + (C)9 * eu * eF);
+      f[q] = feq_q<C>(q, rho, ux, uy, uz, usq15) + keep * f[q] + S;
+    }
+  } else {
+    C taus = tau < (C)0.6 ? (C)0.6 : (tau > (C)1.5 ? (C)1.5 : tau);
+    C fn = sqrt(Fx * Fx + Fy * Fy + Fz * Fz);
+    C sf = fn > (C)10 ? (C)10 / fn : (C)1;
+    C fx = Fx * sf, fy = Fy * sf, fz = Fz * sf;
+    C un = sqrt(ux * ux + uy * uy + uz * uz);
+    C su = un <= (C)0.2 ? (C)1 : (C)0.2 / un;
+    C sx = ux * su, sy = uy * su, sz = uz * su;
+    C uf = sx * fx + sy * fy + sz * fz;
+    C pref = (C)1 - (C)0.5 / taus;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      C S = (C)0;
+      if (fn > (C)1e-15) {
+        C eu = (C)cx(q) * sx + (C)cy(q) * sy + (C)cz(q) * sz;
+        C ef = (C)cx(q) * fx + (C)cy(q) * fy + (C)cz(q) * fz;
+        S = (C)wd(q) * pref * ((C)3 * ef + (C)9 * eu * uf);
+        S = S < (C)-0.5 ? (C)-0.5 : (S > (C)0.5 ? (C)0.5 : S);
+      }
+      f[q] = feq_q<C>(q, rho, ux, uy, uz, usq15) + keep * f[q] + S;
+    }
+  }
+  res.rho = rho;
+  res.ux = ux;
+  res.uy = uy;
+  res.uz = uz;
+  return res;
+}
+
+// LES nu_sgs from central differences of the previous step's velocity u[3][n]
+// (les_turbulence.py:318-380).  Fluid cells are interior, so the 6 neighbours exist.
+template <typename C>
+__device__ __forceinline__ C les_nu_stencil(const KParams& kp, uint32_t c,
+                                            const float* __restrict__ u) {
+  const uint32_t n = kp.n, sx = 1, sy = kp.nx, sz = kp.nxny;
+  const float* ux = u;
+  const float* uy = u + n;
+  const float* uz = u + 2u * n;
+  C dudx = ((C)ux[c + sx] - (C)ux[c - sx]) * (C)0.5, dudy = ((C)ux[c + sy] - (C)ux[c - sy]) * (C)0.5,
+    dudz = ((C)ux[c + sz] - (C)ux[c - sz]) * (C)0.5;
+  C dvdx = ((C)uy[c + sx] - (C)uy[c - sx]) * (C)0.5, dvdy = ((C)uy[c + sy] - (C)uy[c - sy]) * (C)0.5,
+    dvdz = ((C)uy[c + sz] - (C)uy[c - sz]) * (C)0.5;
+  C dwdx = ((C)uz[c + sx] - (C)uz[c - sx]) * (C)0.5, dwdy = ((C)uz[c + sy] - (C)uz[c - sy]) * (C)0.5,
+    dwdz = ((C)uz[c + sz] - (C)uz[c - sz]) * (C)0.5;
+  C S12 = (C)0.5 * (dudy + dvdx), S13 = (C)0.5 * (dudz + dwdx), S23 = (C)0.5 * (dvdz + dwdy);
+  C smag = sqrt((C)2 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz +
+                        (C)2 * (S12 * S12 + S13 * S13 + S23 * S23)));
+  if (smag < (C)kp.strain_floor) return (C)0;
+  C nu = (C)kp.cs2 * smag;
+  return nu < (C)kp.nu_max ? nu : (C)kp.nu_max;
+}
+
+// ---- storage formats ------------------------------------------------------------------------
+template <int S>
+struct Store;
+template <>
+struct Store<POG_STORE_F32> {
+  using E = float;
+  using C = float;
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int, C) { return p[i]; }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int, C v, C) { p[i] = v; }
+};
+template <>
+struct Store<POG_STORE_F64> {
+  using E = double;
+  using C = double;
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int, C) { return p[i]; }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int, C v, C) { p[i] = v; }
+};
+template <>
+struct Store<POG_STORE_F16S> {
+  using E = __half;
+  using C = float;
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C rho0) {
+    return (float)wd(q) * rho0 + __half2float(p[i]) * F16_INV_SCALE;
+  }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C rho0) {
+    p[i] = __float2half_rn((v - (float)wd(q) * rho0) * F16_SCALE);
+  }
+};
+template <>
+struct Store<POG_STORE_BF16S> {
+  using E = __nv_bfloat16;
+  using C = float;
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C rho0) {
+    return (float)wd(q) * rho0 + __bfloat162float(p[i]);
+  }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C rho0) {
+    p[i] = __float2bfloat16_rn(v - (float)wd(q) * rho0);
+  }
+};
+
+// FP64 block reduction of the POG_RED_* slots: warp shuffles, shared memory, one atomic per
+// block and slot.  All threads of the block must call it.
+__device__ __forceinline__ void block_reduce_add(double v[POG_RED_COUNT], double* out) {
+  __shared__ double sm[POG_RED_COUNT][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int r = 0; r < POG_RED_COUNT; ++r) {
+    double x = v[r];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[r][warp] = x;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int r = 0; r < POG_RED_COUNT; ++r) {
+      double x = lane < nw ? sm[r][lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0 && x != 0.0) atomicAdd(out + r, x);
+    }
+  }
+}
+
+}  // namespace pog

@@ -1,0 +1,112 @@
+// lbm_push.cu -- the same step on natural layout with two buffers: each fluid cell collides
+// and pushes f*_q to c + e_q, or into opp(q) of its own cell when c + e_q is solid
+// (legacy/lbm_solver.py:609-628).  Used where every intermediate state must be kept in
+// natural layout: checkpointed recomputation under the adjoint and FP64 reference runs.
+#include "collide.cuh"
+
+namespace pog {
+
+constexpr int PUSH_BLOCK = 256;
+
+template <int S, bool REDUCE>
+__global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
+    const KParams kp, const typename Store<S>::E* __restrict__ fin,
+    typename Store<S>::E* __restrict__ fout, const uint8_t* __restrict__ flags,
+    const float* __restrict__ force, const float* __restrict__ eps,
+    const float* __restrict__ u_prev, float* __restrict__ rho_out, float* __restrict__ u_out,
+    double* __restrict__ red) {
+  using St = Store<S>;
+  using C = typename St::C;
+  const C rho0 = (C)kp.rho0;
+  const uint32_t n = kp.n;
+  double acc[POG_RED_COUNT];
+  if (REDUCE) {
+#pragma unroll
+    for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] = 0.0;
+  }
+  for (uint32_t c = blockIdx.x * PUSH_BLOCK + threadIdx.x; c < n; c += gridDim.x * PUSH_BLOCK) {
+    const uint8_t fl = flags[c];
+    if (fl & POG_CELL_SOLID) continue;
+    C fv[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) fv[q] = St::ld(fin, (uint32_t)q * n + c, q, rho0);
+    C nu_st = (C)0;
+    if (kp.les_mode == POG_LES_STENCIL && u_prev && !(fl & POG_CELL_POROUS))
+      nu_st = les_nu_stencil<C>(kp, c, u_prev);
+    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, eps, nu_st);
+    if (rho_out) rho_out[c] = (float)r.rho;
+    if (u_out) {
+      u_out[c] = (float)r.ux;
+      u_out[n + c] = (float)r.uy;
+      u_out[2u * n + c] = (float)r.uz;
+    }
+    if (REDUCE) {
+      acc[POG_RED_MASS] += (double)r.rho;
+      acc[POG_RED_MOMX] += (double)r.rho * (double)r.ux;
+      acc[POG_RED_MOMY] += (double)r.rho * (double)r.uy;
+      acc[POG_RED_MOMZ] += (double)r.rho * (double)r.uz;
+      acc[POG_RED_OUTFLOW] += (double)r.outflow;
+      const bool bad = !(isfinite((double)r.rho) && isfinite((double)r.ux) &&
+                         isfinite((double)r.uy) && isfinite((double)r.uz));
+      acc[POG_RED_NONFINITE] += bad ? 1.0 : 0.0;
+    }
+    const bool near = (fl & POG_CELL_NEAR_SOLID) != 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const uint32_t dst = c + (uint32_t)kp.off[q];
+      const bool wall = near && q != 0 && (flags[dst] & POG_CELL_SOLID);
+      if (wall)
+        St::st(fout, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
+      else
+        St::st(fout, (uint32_t)q * n + dst, q, fv[q], rho0);
+    }
+  }
+  if (REDUCE) block_reduce_add(acc, red);
+}
+
+template <int S, bool R>
+static int launch_push(const KParams& kp, const void* fin, void* fout, const uint8_t* flags,
+                       const float* force, const float* eps, const float* u_prev, float* rho_out,
+                       float* u_out, double* red, cudaStream_t s) {
+  auto kern = push_step_kernel<S, R>;
+  static thread_local int grid = 0;
+  if (grid == 0) grid = persistent_blocks((const void*)kern, PUSH_BLOCK);
+  if (grid <= 0) return set_error(POG_E_CUDA, "occupancy query failed");
+  int want = (int)((kp.n + PUSH_BLOCK - 1) / PUSH_BLOCK);
+  int g = want < grid ? want : grid;
+  using E = typename Store<S>::E;
+  kern<<<g, PUSH_BLOCK, 0, s>>>(kp, (const E*)fin, (E*)fout, flags, force, eps, u_prev, rho_out,
+                                u_out, red);
+  count_launch();
+  POG_TRY_CUDA(cudaGetLastError());
+  return POG_OK;
+}
+
+}  // namespace pog
+
+using namespace pog;
+
+extern "C" int pog_step_push(const pog_params* p, const void* f_in, void* f_out,
+                             const uint8_t* flags, const float* force, const float* porosity,
+                             const float* u_prev, float* rho_out, float* u_out,
+                             double* reductions, void* stream) {
+  int rc = pog_validate_params(p);
+  if (rc) return rc;
+  if (!f_in || !f_out || !flags) return set_error(POG_E_ARG, "f_in/f_out/flags is NULL");
+  if (f_in == f_out) return set_error(POG_E_ARG, "push step needs distinct f_in and f_out");
+  if (p->les_mode == POG_LES_STENCIL && !u_prev)
+    return set_error(POG_E_ARG, "LES stencil mode needs u_prev");
+  KParams kp = make_kparams(p);
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool R = reductions != nullptr;
+#define POG_PUSH(SS)                                                                              \
+  if (p->storage == SS)                                                                           \
+    return R ? launch_push<SS, true>(kp, f_in, f_out, flags, force, porosity, u_prev, rho_out, u_out, reductions, s) \
+             : launch_push<SS, false>(kp, f_in, f_out, flags, force, porosity, u_prev, rho_out, u_out, reductions, s);
+  POG_PUSH(POG_STORE_F32)
+  POG_PUSH(POG_STORE_F16S)
+  POG_PUSH(POG_STORE_BF16S)
+  POG_PUSH(POG_STORE_F64)
+#undef POG_PUSH
+  return set_error(POG_E_ARG, "storage %d unknown", p->storage);
+}

@@ -1,0 +1,118 @@
+"""GPU adjoint checks.
+
+1. The hand-written CUDA adjoint (FP64 storage) equals the oracle's forward-mode dual-number
+   differentiation of the restated step (committed fixture, 12^3, 12 steps) to 1e-9 relative.
+2. Checkpointed recomputation (every K steps) gives the same gradients as K = T.
+3. Gradients agree with central finite differences (h = 1e-3) of the FP64 forward to 1e-4
+   relative, on the inlet-profile coefficients and on porous cells with non-negligible
+   gradients.
+4. The torch.autograd.Function returns those gradients; the FP32 adjoint is within 1e-3 of FP64.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint, outflow_loss
+from pour_over_coffee_lbm_gb300.params import CELL_POROUS, STORE_F32, STORE_F64, porosity_field
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "oracle_small.npz")
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+
+
+def _case():
+    import make_golden as mg
+    return mg.adjoint_case()
+
+
+def test_adjoint_matches_dual_number_oracle(cuda):
+    g = np.load(GOLD)
+    cfg = _case().replace(storage=STORE_F64)
+    run = OutflowAdjoint(cfg, steps=12, checkpoint_every=4)
+    eps = torch.as_tensor(g["adjoint/eps"]).reshape(cfg.nz, cfg.ny, cfg.nx)
+    J = run.forward(eps, cfg.inlet_coef)
+    res = run.backward()
+    assert abs(J - g["adjoint/loss"][0]) <= 1e-11 * abs(g["adjoint/loss"][0])
+    gi = res.grad_inlet.cpu().numpy()
+    assert np.allclose(gi, g["adjoint/grad_inlet"], rtol=1e-9, atol=1e-18)
+    ge = res.grad_porosity.cpu().numpy()
+    ref = g["adjoint/grad_eps"]
+    assert np.abs(ge - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_checkpointing_is_exact(cuda):
+    cfg = _case().replace(storage=STORE_F64, nx=16, ny=16, nz=16)
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=3)).reshape(cfg.nz, cfg.ny, cfg.nx)
+    a = OutflowAdjoint(cfg, steps=20, checkpoint_every=20)
+    a.forward(eps, cfg.inlet_coef)
+    ra = a.backward()
+    b = OutflowAdjoint(cfg, steps=20, checkpoint_every=3)
+    b.forward(eps, cfg.inlet_coef)
+    rb = b.backward()
+    assert torch.equal(ra.grad_inlet, rb.grad_inlet)
+    assert torch.equal(ra.grad_porosity, rb.grad_porosity)
+
+
+def test_finite_differences(cuda):
+    cfg = _case().replace(storage=STORE_F64, nx=20, ny=20, nz=20, cone_apex_z=3.0, inlet_radius=5.0)
+    T = 40
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=5)).reshape(cfg.nz, cfg.ny, cfg.nx)
+    run = OutflowAdjoint(cfg, steps=T, checkpoint_every=10)
+    run.forward(eps, cfg.inlet_coef)
+    res = run.backward()
+    h = 1e-3
+    coef = np.array(cfg.inlet_coef, np.float64)
+    for k in (0, 1, 5, 15):
+        cp = coef.copy(); cp[k] += h
+        cm = coef.copy(); cm[k] -= h
+        fd = (run.loss(eps, cp) - run.loss(eps, cm)) / (2 * h)
+        ad = res.grad_inlet[k].item()
+        assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-14, (k, ad, fd)
+    ge = res.grad_porosity.cpu().numpy().reshape(-1)
+    band = np.flatnonzero((fl.reshape(-1) & CELL_POROUS) != 0)
+    big = band[np.argsort(-np.abs(ge[band]))[:8]]
+    flat = eps.reshape(-1)
+    for c in big:
+        ep = flat.clone(); ep[c] += h
+        em = flat.clone(); em[c] -= h
+        # eps is float32: use the representable perturbation actually applied
+        hh = (ep[c].double() - em[c].double()).item() / 2
+        fd = (run.loss(ep.reshape(eps.shape), coef) - run.loss(em.reshape(eps.shape), coef)) / (2 * hh)
+        assert abs(ge[c] - fd) <= 1e-4 * abs(fd), (c, ge[c], fd)
+
+
+def test_autograd_function_and_fp32(cuda):
+    cfg = _case().replace(storage=STORE_F64, nx=16, ny=16, nz=16)
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=9)).reshape(cfg.nz, cfg.ny, cfg.nx).cuda().requires_grad_(True)
+    coef = torch.tensor(cfg.inlet_coef, dtype=torch.float64, device="cuda", requires_grad=True)
+    run = OutflowAdjoint(cfg, steps=16, checkpoint_every=4)
+    J = outflow_loss(eps, coef, run)
+    ge, gc = torch.autograd.grad(J, (eps, coef))
+    ref = OutflowAdjoint(cfg, steps=16, checkpoint_every=16)
+    ref.forward(eps.detach(), cfg.inlet_coef)
+    rr = ref.backward()
+    assert torch.allclose(gc, rr.grad_inlet, rtol=1e-12, atol=0)
+    assert torch.allclose(ge.double(), rr.grad_porosity.float().double(), rtol=1e-6, atol=0)
+    r32 = OutflowAdjoint(cfg.replace(storage=STORE_F32), steps=16, checkpoint_every=4)
+    r32.forward(eps.detach(), cfg.inlet_coef)
+    g32 = r32.backward()
+    assert torch.allclose(g32.grad_inlet, rr.grad_inlet, rtol=1e-3, atol=1e-3 * rr.grad_inlet.abs().max().item())
+
+
+def test_adjoint_rejects_unsupported_modes(cuda):
+    from pour_over_coffee_lbm_gb300 import _lib
+    from pour_over_coffee_lbm_gb300.params import LES_STENCIL
+    cfg = _case().replace(storage=STORE_F64, les_mode=LES_STENCIL)
+    run = OutflowAdjoint(cfg, steps=2, checkpoint_every=1)
+    with pytest.raises(_lib.PogError):
+        run.forward(None, cfg.inlet_coef)
+        run.backward()
