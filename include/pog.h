@@ -177,7 +177,10 @@ int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, flo
  *              the call; after an odd nsteps the newest u is in u_next, else in u_prev)
  *   rho_out, u_out  macroscopic output (rho and Guo-corrected u of the incoming state) of
  *              the LAST step, or NULL
- *   reductions POG_RED_COUNT doubles accumulated over all nsteps, or NULL */
+ *   reductions POG_RED_COUNT doubles accumulated over all nsteps, or NULL
+ * Kernel: the TMA-staged step (bulk copies of the 19 planes through a shared-memory ring) when
+ * f is 16-byte aligned, else the register-staged step; the environment variable
+ * POG_AA_KERNEL=plain forces the latter.  Both compute the same update. */
 int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, int nsteps,
              const float* force, const float* porosity, float* u_prev, float* u_next,
              float* rho_out, float* u_out, double* reductions, void* stream);
@@ -201,6 +204,10 @@ int pog_import_natural(const pog_params* p, const void* f_nat, int in_storage,
  * Replaces LBMSolver._compute_macroscopic_quantities (legacy/lbm_solver.py:488-535). */
 int pog_macroscopic(const pog_params* p, const void* f, const uint8_t* flags, long long t,
                     const float* force, float* rho_out, float* u_out, void* stream);
+
+/* Synchronise the device and report whether a kernel raised the device error word (a bounded
+ * mbarrier wait that gave up): POG_OK or POG_E_STATE; `reset` clears the word. */
+int pog_device_status(int reset);
 
 /* ---- particles ----------------------------------------------------------------------------- */
 /* Cell key of every particle, key = i + nx*(j + ny*k) with (i,j,k) = int(clamp(pos, 0, n-2))

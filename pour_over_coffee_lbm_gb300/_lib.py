@@ -40,6 +40,7 @@ SIGNATURES = [
     ("pog_particles_couple", _i, [_P, _PP, _v, _v, _v, _v, _v, _i, _v, _v, _v, _v, _v, _v]),
     ("pog_force_from_fixed", _i, [_P, _v, _v, _v]),
     ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v]),
+    ("pog_device_status", _i, [_i]),
 ]
 
 

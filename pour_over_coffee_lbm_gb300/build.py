@@ -15,10 +15,13 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpog.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# FP32 reciprocal/sqrt/denormal flags apply to single precision only (FP64 paths unaffected)
+FAST_F32 = ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
 SOURCES = {
     "api.cu": [],
     "geometry.cu": ["-fmad=false"],
-    "lbm_aa.cu": [],
+    "lbm_aa.cu": FAST_F32,
+    "lbm_tma.cu": FAST_F32,
     "lbm_push.cu": [],
     "particles.cu": ["-fmad=false"],
     "adjoint.cu": [],

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
   for (int k = 0; k < POG_INLET_NCOEF; ++k) ginl[k] = 0.0;
   for (uint32_t c = blockIdx.x * ADJ_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_BLOCK) {
     const uint8_t fl = flags[c];
-    if (fl & POG_CELL_SOLID) {
+    if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)0;
       continue;

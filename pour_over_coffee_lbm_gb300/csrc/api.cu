@@ -42,6 +42,8 @@ KParams make_kparams(const pog_params* p) {
   k.nz = (uint32_t)p->nz;
   k.nxny = k.nx * k.ny;
   k.n = k.nxny * k.nz;
+  k.guard_lo = k.nxny + k.nx + 1;
+  k.guard_hi = k.n - 1 - k.guard_lo;
   for (int q = 0; q < 19; ++q)
     k.off[q] = cx(q) + cy(q) * (int32_t)k.nx + cz(q) * (int32_t)k.nxny;
   k.les_mode = p->les_mode;

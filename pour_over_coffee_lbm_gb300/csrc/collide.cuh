@@ -1,6 +1,6 @@
-// collide.cuh -- per-cell physics shared by the AA kernel (lbm_aa.cu) and the push kernel
-// (lbm_push.cu): moments, inlet/outlet equilibrium overwrite, Guo forcing with gravity and the
-// external force, Darcy-Forchheimer drag in the filter band, LES relaxation, BGK collision.
+// collide.cuh -- per-cell physics shared by the AA kernels (lbm_aa.cu, lbm_tma.cu) and the push
+// kernel (lbm_push.cu): moments, inlet/outlet equilibrium overwrite, Guo forcing with gravity and
+// the external force, Darcy-Forchheimer drag in the filter band, LES relaxation, BGK collision.
 //
 // Reference structure restated (file:line in latteine1217/pour-over-coffee-lbm):
 //   moments + Guo half-force velocity   src/core/legacy/lbm_solver.py:488-535
@@ -11,6 +11,14 @@
 //   Smagorinsky nu_sgs + gates           src/physics/les_turbulence.py:318-380
 //   Darcy-Forchheimer drag               src/physics/filter_paper.py:471-536
 //   inlet/outlet overwrite               src/physics/boundary_conditions.py:194-324
+//
+// Arithmetic layout (same mathematics as the oracle, arranged for few instructions):
+//   - all moments (rho, m, and the raw second moments for LES) come from one sweep of adds
+//     over shared partial sums;
+//   - the non-equilibrium stress is Pi_neq = sum e e f - rho (u u + I/3), exact for the D3Q19
+//     second-order equilibrium, so no per-direction f_eq pass is needed before tau is known;
+//   - the collision treats each direction q with its opposite together: f_eq and the Guo term
+//     split into a part even in e (shared) and a part odd in e (sign flips), halving the work.
 #pragma once
 #include "common.cuh"
 
@@ -23,7 +31,7 @@ struct CellResult {
 };
 
 template <typename C>
-__device__ __forceinline__ C inlet_uz(const KParams& kp, uint32_t c) {
+__host__ __device__ __forceinline__ C inlet_uz(const KParams& kp, uint32_t c) {
   uint32_t i = c % kp.nx;
   uint32_t j = (c / kp.nx) % kp.ny;
   C dx = (C)i - (C)kp.cxf, dy = (C)j - (C)kp.cyf;
@@ -45,29 +53,44 @@ __device__ __forceinline__ C inlet_uz(const KParams& kp, uint32_t c) {
 }
 
 template <typename C>
-__device__ __forceinline__ C feq_q(int q, C rho, C ux, C uy, C uz, C usq15) {
+__host__ __device__ __forceinline__ C feq_q(int q, C rho, C ux, C uy, C uz, C usq15) {
   C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
   return (C)wd(q) * rho * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - usq15);
+}
+
+// One direction pair (q, opp q) of the BGK + Guo collision, q with e = (ex, ey, ez).
+//   keep = 1 - omega, a1 = omega w rho, b3 = 3 A w (A = 1 - omega/2), b3uF = b3 uF, base = 1 - 1.5 u.u
+template <int Q, typename C>
+__host__ __device__ __forceinline__ void collide_pair(C f[19], C ux, C uy, C uz, C Fx, C Fy, C Fz,
+                                                      C keep, C a1, C b3, C b3uF, C base) {
+  constexpr int P = opp(Q);
+  const C eu = (C)cx(Q) * ux + (C)cy(Q) * uy + (C)cz(Q) * uz;
+  const C eF = (C)cx(Q) * Fx + (C)cy(Q) * Fy + (C)cz(Q) * Fz;
+  // even part: omega feq_s + S_s = a1 (base + 4.5 eu^2) + b3 (3 eu eF - uF)
+  const C sym = a1 * (base + (C)4.5 * eu * eu) + b3 * ((C)3 * eu * eF) - b3uF;
+  // odd part: omega feq_a + S_a = 3 a1 eu + b3 eF
+  const C asym = (C)3 * a1 * eu + b3 * eF;
+  const C fq = f[Q], fp = f[P];
+  f[Q] = keep * fq + (sym + asym);
+  f[P] = keep * fp + (sym - asym);
 }
 
 // f[19]: incoming populations on entry, post-collision populations on exit.
 // nu_st: nu_sgs from the velocity stencil (LES_STENCIL mode), computed by the caller.
 template <typename C>
-__device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t fl, uint32_t c,
-                                                      C f[19], const float* __restrict__ force,
-                                                      const float* __restrict__ eps, C nu_st) {
+__host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t fl, uint32_t c,
+                                                               C f[19], const float* __restrict__ force,
+                                                               const float* __restrict__ eps, C nu_st) {
   CellResult<C> res;
-  C rho = (C)0, mx = (C)0, my = (C)0, mz = (C)0;
-#pragma unroll
-  for (int q = 0; q < 19; ++q) {
-    rho += f[q];
-    if (cx(q) > 0) mx += f[q];
-    if (cx(q) < 0) mx -= f[q];
-    if (cy(q) > 0) my += f[q];
-    if (cy(q) < 0) my -= f[q];
-    if (cz(q) > 0) mz += f[q];
-    if (cz(q) < 0) mz -= f[q];
-  }
+  // ---- moments from one sweep of adds -------------------------------------------------------
+  const C sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
+  const C sxy = (f[7] + f[8]) + (f[9] + f[10]);
+  const C sxz = (f[11] + f[12]) + (f[13] + f[14]);
+  const C syz = (f[15] + f[16]) + (f[17] + f[18]);
+  const C rho = f[0] + (sx + sy) + (sz + sxy) + (sxz + syz);
+  const C mx = (f[1] - f[2]) + ((f[7] - f[8]) + (f[9] - f[10])) + ((f[11] - f[12]) + (f[13] - f[14]));
+  const C my = (f[3] - f[4]) + ((f[7] + f[8]) - (f[9] + f[10])) + ((f[15] - f[16]) + (f[17] - f[18]));
+  const C mz = (f[5] - f[6]) + ((f[11] + f[12]) - (f[13] + f[14])) + ((f[15] + f[16]) - (f[17] + f[18]));
   res.outflow = (C)0;
   if (fl & (POG_CELL_INLET | POG_CELL_OUTLET)) {
     C ux, uy, uz, rr;
@@ -100,7 +123,7 @@ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t
     Gy += (C)force[kp.n + c];
     Gz += (C)force[2u * kp.n + c];
   }
-  C inv_rho = (C)1 / rho;
+  const C inv_rho = (C)1 / rho;
   C ux = (mx + (C)0.5 * Gx) * inv_rho, uy = (my + (C)0.5 * Gy) * inv_rho,
     uz = (mz + (C)0.5 * Gz) * inv_rho;
   C Fx = Gx, Fy = Gy, Fz = Gz;
@@ -150,34 +173,23 @@ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t
       uz = (mz + (C)0.5 * Fz) * inv_rho;
     }
   }
-  const C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
-  // f <- f - f_eq (non-equilibrium part), and the non-equilibrium stress for LES_LOCAL.
-  C Pxx = 0, Pyy = 0, Pzz = 0, Pxy = 0, Pxz = 0, Pyz = 0;
-  const bool les_local = kp.les_mode == POG_LES_LOCAL && !porous;
-#pragma unroll
-  for (int q = 0; q < 19; ++q) {
-    C d = f[q] - feq_q<C>(q, rho, ux, uy, uz, usq15);
-    f[q] = d;
-    if (les_local) {
-      if (cx(q) != 0) Pxx += d;
-      if (cy(q) != 0) Pyy += d;
-      if (cz(q) != 0) Pzz += d;
-      if (cx(q) * cy(q) > 0) Pxy += d;
-      if (cx(q) * cy(q) < 0) Pxy -= d;
-      if (cx(q) * cz(q) > 0) Pxz += d;
-      if (cx(q) * cz(q) < 0) Pxz -= d;
-      if (cy(q) * cz(q) > 0) Pyz += d;
-      if (cy(q) * cz(q) < 0) Pyz -= d;
-    }
-  }
+  const C usq = ux * ux + uy * uy + uz * uz;
   const C tau0 = (C)kp.tau;
   C nu = (C)0;
-  if (les_local) {
-    C PP = Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + (C)2 * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz);
-    C Q = sqrt((C)2 * PP);
-    C tl = (C)0.5 * (tau0 + sqrt(tau0 * tau0 + (C)18 * (C)kp.cs2 * Q * inv_rho));
-    C smag = (C)3 * Q / ((C)2 * rho * tl);
-    nu = (tl - tau0) / (C)3;
+  if (kp.les_mode == POG_LES_LOCAL && !porous) {
+    // Pi_neq = sum e e f - rho (u u + I/3)
+    const C r3 = rho * (C)(1.0 / 3.0);
+    const C Pxx = (sx + sxy + sxz) - (rho * ux * ux + r3);
+    const C Pyy = (sy + sxy + syz) - (rho * uy * uy + r3);
+    const C Pzz = (sz + sxz + syz) - (rho * uz * uz + r3);
+    const C Pxy = ((f[7] - f[8]) - (f[9] - f[10])) - rho * ux * uy;
+    const C Pxz = ((f[11] - f[12]) - (f[13] - f[14])) - rho * ux * uz;
+    const C Pyz = ((f[15] - f[16]) - (f[17] - f[18])) - rho * uy * uz;
+    const C PP = Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + (C)2 * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz);
+    const C Q = sqrt((C)2 * PP);
+    const C tl = (C)0.5 * (tau0 + sqrt(tau0 * tau0 + (C)18 * (C)kp.cs2 * Q * inv_rho));
+    const C smag = (C)1.5 * Q * inv_rho / tl;
+    nu = (tl - tau0) * (C)(1.0 / 3.0);
     if (smag < (C)kp.strain_floor) nu = (C)0;
     nu = nu < (C)kp.nu_max ? nu : (C)kp.nu_max;
   } else if (kp.les_mode == POG_LES_STENCIL && !porous) {
@@ -189,35 +201,47 @@ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t
   const C keep = (C)1 - omega;
 
   if (kp.forcing_mode == POG_FORCING_GUO) {
-    const C pref = (C)1 - (C)0.5 * omega;
+    const C A = (C)1 - (C)0.5 * omega;
     const C uF = ux * Fx + uy * Fy + uz * Fz;
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-      C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
-      C eF = (C)cx(q) * Fx + (C)cy(q) * Fy + (C)cz(q) * Fz;
-      C S = pref * (C)wd(q) * ((C)3 * (eF - uF) + (C)9 * eu * eF);
-      f[q] = feq_q<C>(q, rho, ux, uy, uz, usq15) + keep * f[q] + S;
-    }
+    const C base = (C)1 - (C)1.5 * usq;
+    // weight classes: w0 = 1/3 (rest), w1 = 1/18 (axes), w2 = 1/36 (edges)
+    const C or_ = omega * rho;
+    const C a1_0 = or_ * (C)(1.0 / 3.0), a1_1 = or_ * (C)(1.0 / 18.0), a1_2 = or_ * (C)(1.0 / 36.0);
+    const C b3_0 = A, b3_1 = A * (C)(3.0 / 18.0), b3_2 = A * (C)(3.0 / 36.0);
+    // rest population: f0* = keep f0 + omega w0 rho base - 3 A w0 uF
+    f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF);
+    const C b3uF_1 = b3_1 * uF, b3uF_2 = b3_2 * uF;
+    collide_pair<1, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_1, b3_1, b3uF_1, base);
+    collide_pair<3, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_1, b3_1, b3uF_1, base);
+    collide_pair<5, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_1, b3_1, b3uF_1, base);
+    collide_pair<7, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
+    collide_pair<8, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
+    collide_pair<11, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
+    collide_pair<12, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
+    collide_pair<15, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
+    collide_pair<16, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
   } else {
+    const C usq15 = (C)1.5 * usq;
     C taus = tau < (C)0.6 ? (C)0.6 : (tau > (C)1.5 ? (C)1.5 : tau);
     C fn = sqrt(Fx * Fx + Fy * Fy + Fz * Fz);
     C sf = fn > (C)10 ? (C)10 / fn : (C)1;
     C fx = Fx * sf, fy = Fy * sf, fz = Fz * sf;
-    C un = sqrt(ux * ux + uy * uy + uz * uz);
+    C un = sqrt(usq);
     C su = un <= (C)0.2 ? (C)1 : (C)0.2 / un;
-    C sx = ux * su, sy = uy * su, sz = uz * su;
-    C uf = sx * fx + sy * fy + sz * fz;
+    C sxv = ux * su, syv = uy * su, szv = uz * su;
+    C uf = sxv * fx + syv * fy + szv * fz;
     C pref = (C)1 - (C)0.5 / taus;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
       C S = (C)0;
       if (fn > (C)1e-15) {
-        C eu = (C)cx(q) * sx + (C)cy(q) * sy + (C)cz(q) * sz;
+        C eu = (C)cx(q) * sxv + (C)cy(q) * syv + (C)cz(q) * szv;
         C ef = (C)cx(q) * fx + (C)cy(q) * fy + (C)cz(q) * fz;
         S = (C)wd(q) * pref * ((C)3 * ef + (C)9 * eu * uf);
         S = S < (C)-0.5 ? (C)-0.5 : (S > (C)0.5 ? (C)0.5 : S);
       }
-      f[q] = feq_q<C>(q, rho, ux, uy, uz, usq15) + keep * f[q] + S;
+      const C fe = feq_q<C>(q, rho, ux, uy, uz, usq15);
+      f[q] = fe + keep * (f[q] - fe) + S;
     }
   }
   res.rho = rho;
@@ -230,8 +254,8 @@ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t
 // LES nu_sgs from central differences of the previous step's velocity u[3][n]
 // (les_turbulence.py:318-380).  Fluid cells are interior, so the 6 neighbours exist.
 template <typename C>
-__device__ __forceinline__ C les_nu_stencil(const KParams& kp, uint32_t c,
-                                            const float* __restrict__ u) {
+__host__ __device__ __forceinline__ C les_nu_stencil(const KParams& kp, uint32_t c,
+                                                     const float* __restrict__ u) {
   const uint32_t n = kp.n, sx = 1, sy = kp.nx, sz = kp.nxny;
   const float* ux = u;
   const float* uy = u + n;

@@ -43,6 +43,10 @@ constexpr float F16_INV_SCALE = 1.0f / 4096.0f;
 struct KParams {
   uint32_t nx, ny, nz, n;  // n = nx*ny*nz
   uint32_t nxny;
+  // cells whose 18 neighbours are all inside the grid: guard_lo <= c <= guard_hi.  Kernels
+  // that read neighbours skip cells outside this range whatever the flags say, so a caller's
+  // malformed flags (a fluid cell on the outer shell) cannot drive an access out of bounds.
+  uint32_t guard_lo, guard_hi;
   int32_t off[19];         // neighbour offset of direction q in cells
   int32_t les_mode, drag_mode, forcing_mode, clamp_tau, storage;
   float tau, rho0, gx, gy, gz;

@@ -22,9 +22,17 @@
 namespace pog {
 
 constexpr int AA_BLOCK = 256;
+// Resident-block hint for the step kernel (caps registers per thread) and whether the non-
+// reducing variants run one cell per thread (1) or a persistent grid-stride loop (0).
+#ifndef POG_AA_MINB
+#define POG_AA_MINB 4
+#endif
+#ifndef POG_AA_ONE_CELL
+#define POG_AA_ONE_CELL 1
+#endif
 
 template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
-__global__ void __launch_bounds__(AA_BLOCK) aa_step_kernel(
+__global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
     const KParams kp, typename Store<S>::E* __restrict__ f, const uint8_t* __restrict__ flags,
     const float* __restrict__ force, const float* __restrict__ eps,
     const float* __restrict__ u_prev, float* __restrict__ u_next, float* __restrict__ rho_out,
@@ -40,7 +48,7 @@ __global__ void __launch_bounds__(AA_BLOCK) aa_step_kernel(
   }
   for (uint32_t c = blockIdx.x * AA_BLOCK + threadIdx.x; c < n; c += gridDim.x * AA_BLOCK) {
     const uint8_t fl = flags[c];
-    if (fl & POG_CELL_SOLID) continue;
+    if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
     const bool near = (fl & POG_CELL_NEAR_SOLID) != 0;
     C fv[19];
     if (PARITY == 0) {
@@ -116,7 +124,7 @@ __global__ void aa_export_kernel(const KParams kp, const typename Store<S>::E* _
   const uint32_t n = kp.n;
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
     const uint8_t fl = flags[c];
-    if (fl & POG_CELL_SOLID) {
+    if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) out[(size_t)q * n + c] = (O)0;
       continue;
@@ -183,7 +191,7 @@ static int launch_aa(const KParams& kp, void* f, const uint8_t* flags, const flo
   if (grid == 0) grid = persistent_blocks((const void*)kern, AA_BLOCK);
   if (grid <= 0) return set_error(POG_E_CUDA, "occupancy query failed");
   int want = (int)((kp.n + AA_BLOCK - 1) / AA_BLOCK);
-  int g = want < grid ? want : grid;
+  int g = (POG_AA_ONE_CELL && !REDUCE) ? want : (want < grid ? want : grid);
   kern<<<g, AA_BLOCK, 0, s>>>(kp, (typename Store<S>::E*)f, flags, force, eps, u_prev, u_next,
                               rho_out, u_out, red);
   count_launch();
@@ -224,6 +232,21 @@ static int dispatch_storage(const KParams& kp, int parity, bool reduce, bool mac
       return dispatch_aa<POG_STORE_F64>(kp, parity, reduce, macro, f, flags, force, eps, u_prev, u_next, rho_out, u_out, red, s);
   }
   return set_error(POG_E_ARG, "storage %d unknown", kp.storage);
+}
+
+int launch_aa_tma(const KParams& kp, int parity, bool reduce, void* f, const uint8_t* flags,
+                  const float* force, const float* eps, const float* u_prev, float* u_next,
+                  float* rho_out, float* u_out, double* red, cudaStream_t s);
+
+// Which step kernel pog_step uses: the TMA-staged one (default; needs a 16-byte aligned
+// distribution buffer) or the register-staged one (POG_AA_KERNEL=plain, kept for A/B timing).
+static bool use_tma(const void* f) {
+  static int mode = -1;
+  if (mode < 0) {
+    const char* e = getenv("POG_AA_KERNEL");
+    mode = (e && e[0] == 'p') ? 0 : 1;
+  }
+  return mode == 1 && ((uintptr_t)f & 15u) == 0;
 }
 
 static int grid_for(uint32_t n, int block) {
@@ -287,10 +310,15 @@ int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, in
   for (int i = 0; i < nsteps; ++i) {
     const bool last = i == nsteps - 1;
     const int parity = (int)((t + i) & 1);
-    rc = dispatch_storage(kp, parity, reductions != nullptr, false, f, flags, force, porosity,
-                          stencil ? up : nullptr, stencil ? un : nullptr,
-                          last ? rho_out : nullptr, last ? u_out : nullptr,
-                          reductions, s);
+    if (use_tma(f))
+      rc = launch_aa_tma(kp, parity, reductions != nullptr, f, flags, force, porosity,
+                         stencil ? up : nullptr, stencil ? un : nullptr, last ? rho_out : nullptr,
+                         last ? u_out : nullptr, reductions, s);
+    else
+      rc = dispatch_storage(kp, parity, reductions != nullptr, false, f, flags, force, porosity,
+                            stencil ? up : nullptr, stencil ? un : nullptr,
+                            last ? rho_out : nullptr, last ? u_out : nullptr,
+                            reductions, s);
     if (rc) return rc;
     if (stencil) {
       float* tmp = up;

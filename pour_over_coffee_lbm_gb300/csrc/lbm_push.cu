@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
   }
   for (uint32_t c = blockIdx.x * PUSH_BLOCK + threadIdx.x; c < n; c += gridDim.x * PUSH_BLOCK) {
     const uint8_t fl = flags[c];
-    if (fl & POG_CELL_SOLID) continue;
+    if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
     C fv[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) fv[q] = St::ld(fin, (uint32_t)q * n + c, q, rho0);

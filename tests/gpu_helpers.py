@@ -84,6 +84,7 @@ def run_aa(cfg, steps, eps=None, force=None, reduce=True):
         r.step(steps - 1, reduce=reduce, macro=False)
     r.step(1, reduce=reduce, macro=True)
     torch.cuda.synchronize()
+    assert lib().pog_device_status(1) == 0, lib().pog_last_error()
     return r
 
 

@@ -68,9 +68,13 @@ def test_les_stencil_solver_matches_oracle(cuda, orc):
     _ = s.u.to_numpy()  # reading the accessor must not disturb the LES velocity history
     s.run(1, want_macro=True)
     flags, f, rho, u = orc.run(cfg, 30, np.float32)
+    _, _, _, u64 = orc.run(cfg.replace(storage=3), 30, np.float64)
     fluid = (flags & CELL_SOLID) == 0
     gu = s._u.cpu().numpy()
-    assert np.linalg.norm(gu[:, fluid] - u[:, fluid]) / np.linalg.norm(u[:, fluid]) < 1e-5
+    # FP32 bar: within 2x the FP32 oracle's own error against the FP64 oracle
+    e_orc = np.linalg.norm(u[:, fluid] - u64[:, fluid]) / np.linalg.norm(u64[:, fluid])
+    assert np.linalg.norm(gu[:, fluid] - u64[:, fluid]) / np.linalg.norm(u64[:, fluid]) <= 2 * e_orc + 1e-7
+    assert np.linalg.norm(gu[:, fluid] - u[:, fluid]) / np.linalg.norm(u[:, fluid]) <= 2 * e_orc + 1e-7
 
 
 def test_two_way_coupled_steps_vs_oracle(cuda, orc):
