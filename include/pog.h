@@ -218,6 +218,19 @@ size_t pog_particles_bin_scratch_bytes(int np);
 int pog_particles_bin(const pog_params* p, const float* pos, const int32_t* active, int np,
                       int32_t* keys, int32_t* perm, void* scratch, void* stream);
 
+/* Same binning and stable cell sort as pog_particles_bin, but it allocates nothing and takes
+ * no scratch argument: for callers that may not allocate device memory once running (a host
+ * application that gives the library a fixed device-memory budget, or a loop that must not block
+ * on an allocator).  Its scratch is a fixed device array inside libpog.so, reserved on every GPU
+ * that loads the library until the process exits.  Limit: np <= POG_NOALLOC_MAX_PARTICLES
+ * (larger np returns POG_E_RANGE).  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU race and must be
+ * ordered by the caller.  No counterpart in the reference (it has no sort and no scratch). */
+#define POG_NOALLOC_MAX_PARTICLES (1 << 20)
+int pog_particles_bin_noalloc(const pog_params* p, const float* pos, const int32_t* active, int np,
+                              int32_t* keys, int32_t* perm, void* stream);
+
 /* One two-way coupling pass (LBMSolver.step_with_two_way_coupling, legacy/lbm_solver.py:
  * 1485-1509, with CoffeeParticleSystem.compute_two_way_coupling_forces 1107-1154,
  * apply_under_relaxation 1200-1212 and update_particle_physics 641-720): for each active

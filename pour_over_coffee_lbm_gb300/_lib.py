@@ -41,6 +41,7 @@ SIGNATURES = [
     ("pog_force_from_fixed", _i, [_P, _v, _v, _v]),
     ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_device_status", _i, [_i]),
+    ("pog_particles_bin_noalloc", _i, [_P, _v, _v, _i, _v, _v, _v]),
 ]
 
 

@@ -24,6 +24,7 @@ SOURCES = {
     "lbm_tma.cu": FAST_F32,
     "lbm_push.cu": [],
     "particles.cu": ["-fmad=false"],
+    "particles_noalloc.cu": [],
     "adjoint.cu": [],
 }
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
