@@ -145,12 +145,12 @@ def time_graph(graph, replays):
 
 def kernel_roofline(cfg, steps, peak):
     """Average duration of the fused LBM step kernel alone (same arguments as inside the coupled
-    step: external force read, rho/u write), over `steps` graph-replayed launches."""
+    step: particle drag deposit read, rho/u write), over `steps` graph-replayed launches."""
     import torch
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     s = GB300LBMSolver(cfg)
-    s._force.normal_(0.0, 1e-7)
-    s._force_active = True
+    s._pdrag.uniform_(0.0, 1e-3)
+    s._pdrag_active = True
     for _ in range(4):
         s.run(1, want_macro=True)
     torch.cuda.synchronize()
@@ -161,11 +161,11 @@ def kernel_roofline(cfg, steps, peak):
     per_launch = dt / (reps * GRAPH_STEPS)
     nf = fluid_cells(s.flags)
     esize = s._f.element_size()
-    bytes_per_launch = nf * (2 * 19 * esize + 12 + 4 + 12) + s.n * 1
+    bytes_per_launch = nf * (2 * 19 * esize + 16 + 4 + 12) + s.n * 4
     achieved = bytes_per_launch / per_launch / 1e9
     out = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0], "unit": "GB/s",
            "frac": round(achieved / peak[0], 4), "peak_source": peak[1],
-           "kernel": "aa_step_kernel (fused collide-stream, force read, rho/u write)",
+           "kernel": "aa_step_kernel (fused collide-stream, particle drag read, rho/u write)",
            "kernel_us": round(per_launch * 1e6, 2), "algorithmic_bytes_per_launch": bytes_per_launch,
            "fluid_cells": nf, "cells": s.n}
     del s, g
@@ -219,7 +219,7 @@ def precision_line(storage, steps, peak):
     per = dt / (reps * GRAPH_STEPS)
     nf = fluid_cells(s.flags)
     esize = s._f.element_size()
-    bpl = nf * 2 * 19 * esize + s.n
+    bpl = nf * 2 * 19 * esize + s.n * 4
     mlups = s.n / per / 1e6
     ach = bpl / per / 1e9
     out = {"mlups": round(mlups, 1), "kernel_us": round(per * 1e6, 2), "achieved_gbs": round(ach, 1),
@@ -272,8 +272,8 @@ def cpu_baseline(cfg, pc, seconds):
     t0 = time.perf_counter()
     while True:
         pos, vel, drag, act, fix, _ = O.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
-        force = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(3, cfg.nz, cfg.ny, cfg.nx)
-        f, rho, u = O.step(cfg, flags, f, force=force)
+        pdrag = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(4, cfg.nz, cfg.ny, cfg.nx)
+        f, rho, u = O.step(cfg, flags, f, pdrag=pdrag)
         steps += 1
         el = time.perf_counter() - t0
         if el >= seconds or steps >= 500:
@@ -444,8 +444,8 @@ def run_reference(args):
     def one():
         nonlocal pos, vel, drag, act, f, u
         pos, vel, drag, act, fix, _ = O.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
-        force = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(3, cfg.nz, cfg.ny, cfg.nx)
-        f, _, u = O.step(cfg, flags, f, force=force)
+        pdrag = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(4, cfg.nz, cfg.ny, cfg.nx)
+        f, _, u = O.step(cfg, flags, f, pdrag=pdrag)
 
     W = max(3, args.warmup)
     t0 = time.perf_counter()

@@ -44,7 +44,10 @@ extern "C" {
 #define POG_E_RANGE (-5)    /* a size is beyond a documented limit                           */
 #define POG_E_STATE (-6)    /* call sequence error (e.g. odd AA parity where even required)  */
 
-/* ---- cell flag bits (one uint8 per cell) ------------------------------------------------- */
+/* ---- cell flag word (one uint32 per cell) --------------------------------------------------
+ * Low byte: the cell's own flags below.  Bit POG_LINK_SHIFT + q (q = 1..18) is set when the
+ * neighbour c + e_q is solid, so bounce-back needs no neighbour reads in the step kernels. */
+#define POG_LINK_SHIFT 8
 #define POG_CELL_SOLID 0x01u      /* half-way bounce-back wall (filter_paper.py:206-286)     */
 #define POG_CELL_INLET 0x02u      /* fixed-velocity inlet disk (equilibrium at rho_local)    */
 #define POG_CELL_OUTLET 0x04u     /* pressure outlet under the apex hole (equilibrium rho_out)*/
@@ -133,7 +136,7 @@ typedef struct pog_particle_params {
   float relaxation;     /* under-relaxation alpha of the drag force (lbm_solver.py:1485: 0.8)  */
   float dt;             /* particle time step (lattice units)                                 */
   int32_t drag_model;   /* 0 Stokes, 1 Schiller-Naumann correction (coffee_particles.py:1088)  */
-  int32_t deterministic;/* 1: fixed-point integer accumulation of the spread force            */
+  int32_t deterministic;/* 1: fixed-point integer accumulation of the drag deposit           */
   float wall_margin;    /* radial limit as a fraction of the cone radius (0.9)                 */
   float wall_pullback;  /* radius a violating particle is moved to, fraction (0.8)             */
   float wall_damping;   /* velocity factor on a wall hit (0.3)                                 */
@@ -154,13 +157,13 @@ int pog_validate_params(const pog_params* p);
  * Replaces FilterPaperSystem._setup_v60_geometry / _setup_filter_zones
  * (filter_paper.py:206-364) and the LES mask copy (filter_paper.py:199-204).  Computed in FP64
  * without contraction: the result is bit-exact with the CPU restatement. */
-int pog_build_flags(const pog_params* p, uint8_t* flags, void* stream);
+int pog_build_flags(const pog_params* p, uint32_t* flags, void* stream);
 
 /* ---- distributions --------------------------------------------------------------------------- */
 /* f := equilibrium(rho0, u0) on every non-solid cell, 0 on solid cells, in the storage format
  * of p->storage.  The state is left at AA parity 0 (natural layout).
  * Replaces LBMSolver.init_fields (legacy/lbm_solver.py:1067-1112). */
-int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, float rho0,
+int pog_init_equilibrium(const pog_params* p, void* f, const uint32_t* flags, float rho0,
                          float ux, float uy, float uz, void* stream);
 
 /* Advance `nsteps` time steps in place (AA pattern: one distribution buffer).  `t` is the time
@@ -170,7 +173,10 @@ int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, flo
  * streaming with half-way bounce-back (:537-628), the filter-band Darcy-Forchheimer drag
  * (filter_paper.py:471-536), the particle reaction force (:1478-1483) and the inlet/outlet
  * boundary overwrite (boundary_conditions.py:384-409), fused into one pass per step.
- *   force      [3][ncell] external force density (particle reaction, plugins) or NULL
+ *   force      [3][ncell] explicit external force density (plugins, pouring) or NULL
+ *   pdrag      [4][ncell] particle drag deposit of pog_particles_couple (Kp, Kv) or NULL; the
+ *              particle force Kv - Kp u enters implicitly (add_particle_reaction_forces,
+ *              legacy/lbm_solver.py:1478-1483)
  *   porosity   [ncell] per-cell eps for porous cells, or NULL (uniform p->porosity)
  *   u_prev/u_next [3][ncell] velocity ping-pong buffers: required for POG_LES_STENCIL (step s
  *              reads u_prev and writes u_next; the pointers are swapped every step inside
@@ -178,32 +184,32 @@ int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, flo
  *   rho_out, u_out  macroscopic output (rho and Guo-corrected u of the incoming state) of
  *              the LAST step, or NULL
  *   reductions POG_RED_COUNT doubles accumulated over all nsteps, or NULL
- * Kernel: the TMA-staged step (bulk copies of the 19 planes through a shared-memory ring) when
- * f is 16-byte aligned, else the register-staged step; the environment variable
- * POG_AA_KERNEL=plain forces the latter.  Both compute the same update. */
-int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, int nsteps,
-             const float* force, const float* porosity, float* u_prev, float* u_next,
+ * Kernel: the register-staged step; the environment variable POG_AA_KERNEL=tma selects the
+ * TMA-staged step (bulk copies of the 19 planes through a shared-memory ring, warp-specialised)
+ * when f is 16-byte aligned.  Both compute the same update. */
+int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, int nsteps,
+             const float* force, const float* pdrag, const float* porosity, float* u_prev, float* u_next,
              float* rho_out, float* u_out, double* reductions, void* stream);
 
 /* Same step on the natural (two-buffer) layout: reads f_in at time t, writes f_out at t+1
  * with push streaming exactly as legacy/lbm_solver.py:609-628.  Used for checkpointed
  * recomputation under the adjoint and for FP64 reference runs. */
-int pog_step_push(const pog_params* p, const void* f_in, void* f_out, const uint8_t* flags,
-                  const float* force, const float* porosity, const float* u_prev,
+int pog_step_push(const pog_params* p, const void* f_in, void* f_out, const uint32_t* flags,
+                  const float* force, const float* pdrag, const float* porosity, const float* u_prev,
                   float* rho_out, float* u_out, double* reductions, void* stream);
 
 /* Copy the AA state at time t into natural layout (f_nat[q][c] = f_q at cell c), converting
  * the storage format to `out_storage` (POG_STORE_F32 or POG_STORE_F64). */
-int pog_export_natural(const pog_params* p, const void* f, const uint8_t* flags, long long t,
+int pog_export_natural(const pog_params* p, const void* f, const uint32_t* flags, long long t,
                        void* f_nat, int out_storage, void* stream);
 /* Inverse at an even t: natural FP32/FP64 -> AA state in p->storage. */
 int pog_import_natural(const pog_params* p, const void* f_nat, int in_storage,
-                       const uint8_t* flags, void* f, void* stream);
+                       const uint32_t* flags, void* f, void* stream);
 
 /* Density and Guo-corrected velocity of the AA state at time t, without advancing it.
  * Replaces LBMSolver._compute_macroscopic_quantities (legacy/lbm_solver.py:488-535). */
-int pog_macroscopic(const pog_params* p, const void* f, const uint8_t* flags, long long t,
-                    const float* force, float* rho_out, float* u_out, void* stream);
+int pog_macroscopic(const pog_params* p, const void* f, const uint32_t* flags, long long t,
+                    const float* force, const float* pdrag, float* rho_out, float* u_out, void* stream);
 
 /* Synchronise the device and report whether a kernel raised the device error word (a bounded
  * mbarrier wait that gave up): POG_OK or POG_E_STATE; `reset` clears the word. */
@@ -235,18 +241,23 @@ int pog_particles_bin_noalloc(const pog_params* p, const float* pos, const int32
  * 1485-1509, with CoffeeParticleSystem.compute_two_way_coupling_forces 1107-1154,
  * apply_under_relaxation 1200-1212 and update_particle_physics 641-720): for each active
  * particle, trilinear u at its position, drag, under-relaxation of the drag, spreading of the
- * relaxed reaction -F onto the 8 surrounding nodes, then velocity/position update with the
- * cone constraint.  `order` (nullable) lists the particles in processing order (the `perm` of
- * pog_particles_bin) so neighbouring lanes hit neighbouring cells.
- *   force     [3][ncell] float accumulator (fast mode; caller zeroes it), or
- *   force_fix [3][ncell] int64 fixed-point accumulator, scale 2^32 (deterministic mode) */
+ * velocity/position update with the cone constraint, then the particle's drag coefficient
+ * beta = m_p/(tau_p + dt) and beta*v_new are deposited onto the 8 surrounding nodes with the
+ * trilinear weights (Kp = sum w beta, Kv = sum w beta v).  pog_step applies the particle force
+ * on the fluid, Kv - Kp u, implicitly in u, which stays stable where particles pile up (the
+ * reference spreads the explicit reaction -F, distribute_force_to_grid 1048-1086, which
+ * diverges once the particle mass in a cell exceeds the fluid's).  `order` (nullable) lists
+ * the particles in processing order (the `perm` of pog_particles_bin) so neighbouring lanes
+ * hit neighbouring cells.
+ *   pdrag     [4][ncell] float accumulator (Kp, Kv_x, Kv_y, Kv_z; fast mode; caller zeroes), or
+ *   pdrag_fix [4][ncell] int64 fixed-point accumulator, scale 2^32 (deterministic mode) */
 int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, float* pos,
                          float* vel, const float* diameter, float* drag_old, int32_t* active,
-                         int np, const int32_t* order, const float* u, float* force,
-                         long long* force_fix, float* u_at_particle, void* stream);
-/* force[a][c] = force_fix[a][c] * 2^-32 (deterministic-mode conversion). */
-int pog_force_from_fixed(const pog_params* p, const long long* force_fix, float* force,
-                         void* stream);
+                         int np, const int32_t* order, const float* u, float* pdrag,
+                         long long* pdrag_fix, float* u_at_particle, void* stream);
+/* pdrag[a][c] = pdrag_fix[a][c] * 2^-32, a = 0..3 (deterministic-mode conversion). */
+int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* pdrag,
+                        void* stream);
 
 /* ---- adjoint --------------------------------------------------------------------------------- */
 /* Reverse of one pog_step_push step (natural layout, storage F32 or F64).
@@ -257,7 +268,7 @@ int pog_force_from_fixed(const pog_params* p, const long long* force_fix, float*
  *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
  *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL. */
 int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next, void* lam_t,
-                     const uint8_t* flags, const float* porosity, double* grad_porosity,
+                     const uint32_t* flags, const float* porosity, double* grad_porosity,
                      double* grad_inlet, void* stream);
 
 #ifdef __cplusplus

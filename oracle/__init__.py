@@ -69,7 +69,7 @@ def tables():
 def build_flags(cfg) -> np.ndarray:
     lib = load()
     _, pp = _params(cfg)
-    flags = np.zeros((cfg.nz, cfg.ny, cfg.nx), np.uint8)
+    flags = np.zeros((cfg.nz, cfg.ny, cfg.nx), np.uint32)
     lib.orc_build_flags(pp, _p(flags))
     return flags
 
@@ -86,8 +86,9 @@ def init_equilibrium(cfg, flags, dtype=np.float64, rho0=None, u0=(0.0, 0.0, 0.0)
     return f
 
 
-def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None):
-    """One push step.  Returns (f_next, rho, u)."""
+def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdrag=None):
+    """One push step.  force: [3][n] explicit force; pdrag: [4][n] particle drag deposit
+    (Kp, Kv).  Returns (f_next, rho, u)."""
     lib = load()
     _, pp = _params(cfg)
     dt = f.dtype
@@ -98,10 +99,13 @@ def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None):
         force = np.ascontiguousarray(force, np.float32)
     if eps is not None:
         eps = np.ascontiguousarray(eps, np.float32)
+    if pdrag is not None:
+        pdrag = np.ascontiguousarray(pdrag, np.float32)
     if u_prev is not None:
         u_prev = np.ascontiguousarray(u_prev, dt)
     fn = lib.orc_step_f64 if dt == np.float64 else lib.orc_step_f32
-    fn(pp, _p(flags), _p(f), _p(fo), _p(force), _p(eps), _p(u_prev), _p(rho), _p(u), _p(reductions))
+    fn(pp, _p(flags), _p(f), _p(fo), _p(force), _p(pdrag), _p(eps), _p(u_prev), _p(rho), _p(u),
+       _p(reductions))
     return fo, rho, u
 
 
@@ -190,7 +194,8 @@ def particles_bin(cfg, pos, active):
 
 def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=None):
     """One coupling pass (serial, id order) on copies of the state.  Returns the updated
-    (pos, vel, drag_old, active, force_fix, u_at)."""
+    (pos, vel, drag_old, active, force_fix, u_at); force_fix is the [4][n] int64 drag deposit
+    (Kp, Kv) scaled by 2^32."""
     lib = load()
     _, pp = _params(cfg)
     ppp = pcfg.to_c()
@@ -202,7 +207,7 @@ def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=N
     u = np.ascontiguousarray(u, np.float32)
     n = diam.shape[0]
     if force_fix is None:
-        force_fix = np.zeros(3 * cfg.ncell, np.int64)
+        force_fix = np.zeros(4 * cfg.ncell, np.int64)
     u_at = np.zeros((3, n), np.float32)
     lib.orc_particles_couple(pp, ctypes.byref(ppp), _p(pos), _p(vel), _p(diam), _p(drag_old),
                              _p(active), n, _p(u), _p(force_fix), _p(u_at))

@@ -157,7 +157,7 @@ void porous_coeffs(const pog_params* p, T eps, T& K, T& CF) {
 // LES nu_sgs from central differences of a stored velocity field
 // (les_turbulence.py:318-380).  u is [3][n].  Returns 0 where the reference does.
 template <typename T>
-T les_nu_stencil(const pog_params* p, const Geo& g, const uint8_t* flags, const T* u, int i,
+T les_nu_stencil(const pog_params* p, const Geo& g, const uint32_t* flags, const T* u, int i,
                  int j, int k) {
   if (i < 1 || j < 1 || k < 1 || i > g.nx - 2 || j > g.ny - 2 || k > g.nz - 2) return 0;
   long long c = g.idx(i, j, k);
@@ -189,9 +189,9 @@ T les_nu_stencil(const pog_params* p, const Geo& g, const uint8_t* flags, const 
 // Inputs: incoming populations f, flag, optional external force Fe and porosity.  Output:
 // post-collision populations fs, rho, u, and reduction contributions.
 template <typename T>
-void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int k, const T f[19],
-             const T* Fe, bool has_eps, T eps, T nu_stencil, T fs[19], T& rho_o, T u_o[3],
-             double* red, const T* coef = nullptr) {
+void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int k, const T f[19],
+             const T* Fe, const T* Pd, bool has_eps, T eps, T nu_stencil, T fs[19], T& rho_o,
+             T u_o[3], double* red, const T* coef = nullptr) {
   T rho = 0, mx = 0, my = 0, mz = 0;
   for (int q = 0; q < 19; ++q) {
     rho += f[q];
@@ -221,7 +221,17 @@ void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int 
       Gy += Fe[1];
       Gz += Fe[2];
     }
-    T vx = (mx + (T)0.5 * Gx) / rho, vy = (my + (T)0.5 * Gy) / rho, vz = (mz + (T)0.5 * Gz) / rho;
+    // particle drag deposit Pd = (Kp, Kv): fluid force Kv - Kp u, implicit in u
+    T Kp = 0, Kvx = 0, Kvy = 0, Kvz = 0;
+    if (Pd) {
+      Kp = Pd[0];
+      Kvx = Pd[1];
+      Kvy = Pd[2];
+      Kvz = Pd[3];
+    }
+    T A = (T)1 + (T)0.5 * Kp / rho;
+    T vx = (mx + (T)0.5 * (Gx + Kvx)) / rho, vy = (my + (T)0.5 * (Gy + Kvy)) / rho,
+      vz = (mz + (T)0.5 * (Gz + Kvz)) / rho;
     T Fx = Gx, Fy = Gy, Fz = Gz;
     ux = vx;
     uy = vy;
@@ -238,7 +248,8 @@ void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int 
       }
       T sK = sqrt(K);
       if (p->drag_mode == POG_DRAG_SEMI_IMPLICIT) {
-        T c0 = (T)0.5 * ((T)1 + (T)0.5 * nu0 / K);
+        // u (A + nu/(2K) + C_F |u| / (2 sqrt K)) = v
+        T c0 = (T)0.5 * (A + (T)0.5 * nu0 / K);
         T c1 = (T)0.5 * CF / sK;
         T vm = sqrt(vx * vx + vy * vy + vz * vz);
         T s = (T)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
@@ -247,13 +258,14 @@ void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int 
         uz = vz * s;
         T um = sqrt(ux * ux + uy * uy + uz * uz);
         T coef = rho * (nu0 / K + CF / sK * um);
-        Fx = Gx - coef * ux;
-        Fy = Gy - coef * uy;
-        Fz = Gz - coef * uz;
+        Fx = Gx + Kvx - (coef + Kp) * ux;
+        Fy = Gy + Kvy - (coef + Kp) * uy;
+        Fz = Gz + Kvz - (coef + Kp) * uz;
       } else {
-        T vm = sqrt(vx * vx + vy * vy + vz * vz);
+        T wx = vx / A, wy = vy / A, wz = vz / A;  // velocity before the porous drag
+        T vm = sqrt(wx * wx + wy * wy + wz * wz);
         T coef = rho * (nu0 / K + CF / sK * vm);
-        T dx = -coef * vx, dy = -coef * vy, dz = -coef * vz;
+        T dx = -coef * wx, dy = -coef * wy, dz = -coef * wz;
         T dm = sqrt(dx * dx + dy * dy + dz * dz);
         T cap = (T)p->drag_cap;
         if (dm > cap) {
@@ -262,13 +274,20 @@ void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int 
           dy *= sc;
           dz *= sc;
         }
-        Fx = Gx + dx;
-        Fy = Gy + dy;
-        Fz = Gz + dz;
-        ux = (mx + (T)0.5 * Fx) / rho;
-        uy = (my + (T)0.5 * Fy) / rho;
-        uz = (mz + (T)0.5 * Fz) / rho;
+        ux = (mx + (T)0.5 * (Gx + dx + Kvx)) / (rho * A);
+        uy = (my + (T)0.5 * (Gy + dy + Kvy)) / (rho * A);
+        uz = (mz + (T)0.5 * (Gz + dz + Kvz)) / (rho * A);
+        Fx = Gx + dx + Kvx - Kp * ux;
+        Fy = Gy + dy + Kvy - Kp * uy;
+        Fz = Gz + dz + Kvz - Kp * uz;
       }
+    } else if (Pd) {
+      ux = vx / A;
+      uy = vy / A;
+      uz = vz / A;
+      Fx = Gx + Kvx - Kp * ux;
+      Fy = Gy + Kvy - Kp * uy;
+      Fz = Gz + Kvz - Kp * uz;
     }
     equilibrium<T>(rho, ux, uy, uz, feq);
     T tau0 = (T)p->tau;
@@ -350,8 +369,8 @@ void collide(const pog_params* p, const Geo& g, uint8_t flag, int i, int j, int 
 // One push step on natural layout (legacy/lbm_solver.py:460-486 + :609-628): every fluid
 // cell collides and pushes f*_q to x+e_q, or into opp(q) at x when x+e_q is solid.
 template <typename T>
-int step_push(const pog_params* p, const uint8_t* flags, const T* f, T* fo, const float* Fe,
-              const float* eps, const T* u_prev, T* rho_out, T* u_out, double* red) {
+int step_push(const pog_params* p, const uint32_t* flags, const T* f, T* fo, const float* Fe,
+              const float* Pd, const float* eps, const T* u_prev, T* rho_out, T* u_out, double* red) {
   Geo g = make_geo(p);
   const long long n = g.n;
   double acc[POG_RED_COUNT] = {0, 0, 0, 0, 0, 0};
@@ -364,7 +383,7 @@ int step_push(const pog_params* p, const uint8_t* flags, const T* f, T* fo, cons
       for (int j = 0; j < g.ny; ++j)
         for (int i = 0; i < g.nx; ++i) {
           long long c = g.idx(i, j, k);
-          uint8_t fl = flags[c];
+          uint32_t fl = flags[c];
           if (fl & POG_CELL_SOLID) continue;
           T fin[19], fs[19], rho, u[3];
           for (int q = 0; q < 19; ++q) fin[q] = f[q * n + c];
@@ -376,11 +395,17 @@ int step_push(const pog_params* p, const uint8_t* flags, const T* f, T* fo, cons
             fe[2] = (T)Fe[2 * n + c];
             fep = fe;
           }
+          T pd[4];
+          const T* pdp = nullptr;
+          if (Pd) {
+            for (int a = 0; a < 4; ++a) pd[a] = (T)Pd[a * n + c];
+            pdp = pd;
+          }
           T nus = 0;
           if (p->les_mode == POG_LES_STENCIL && u_prev)
             nus = les_nu_stencil<T>(p, g, flags, u_prev, i, j, k);
-          collide<T>(p, g, fl, i, j, k, fin, fep, eps != nullptr, eps ? (T)eps[c] : (T)0, nus, fs,
-                     rho, u, red ? loc : nullptr);
+          collide<T>(p, g, fl, i, j, k, fin, fep, pdp, eps != nullptr, eps ? (T)eps[c] : (T)0, nus,
+                     fs, rho, u, red ? loc : nullptr);
           if (rho_out) rho_out[c] = rho;
           if (u_out) {
             u_out[c] = u[0];
@@ -405,7 +430,7 @@ int step_push(const pog_params* p, const uint8_t* flags, const T* f, T* fo, cons
 }
 
 template <typename T>
-void init_eq(const pog_params* p, const uint8_t* flags, T* f, T rho0, T ux, T uy, T uz) {
+void init_eq(const pog_params* p, const uint32_t* flags, T* f, T rho0, T ux, T uy, T uz) {
   Geo g = make_geo(p);
   T feq[19];
   equilibrium<T>(rho0, ux, uy, uz, feq);
@@ -435,7 +460,7 @@ int orc_d3q19_tables(int* cx, int* cy, int* cz, int* opp, double* w) {
 // the cone wall (rc, rc + wall] minus the hole bore.  Inlet disk on k = nz-2, outlet disk on
 // k = 1.  Porous band: fluid cells at/above the apex inside the wall within band_thickness of
 // it (this includes the hole bore, which the filter paper covers).
-int orc_build_flags(const pog_params* p, uint8_t* flags) {
+int orc_build_flags(const pog_params* p, uint32_t* flags) {
   if (p->inlet_control) return -1;  // device pointer: not readable by the CPU restatement
   Geo g = make_geo(p);
   const double apex = p->cone_apex_z, wall = p->cone_wall, hole = p->hole_radius;
@@ -460,7 +485,7 @@ int orc_build_flags(const pog_params* p, uint8_t* flags) {
     for (int j = 0; j < g.ny; ++j)
       for (int i = 0; i < g.nx; ++i) {
         long long c = g.idx(i, j, k);
-        uint8_t fl = 0;
+        uint32_t fl = 0;
         if (solid[c]) {
           flags[c] = POG_CELL_SOLID;
           continue;
@@ -475,18 +500,18 @@ int orc_build_flags(const pog_params* p, uint8_t* flags) {
             r <= rc + wall)
           fl |= POG_CELL_POROUS;
         for (int q = 1; q < 19; ++q)
-          if (solid[g.idx(i + CX[q], j + CY[q], k + CZ[q])]) fl |= POG_CELL_NEAR_SOLID;
+          if (solid[g.idx(i + CX[q], j + CY[q], k + CZ[q])]) fl |= POG_CELL_NEAR_SOLID | (1u << (POG_LINK_SHIFT + q));
         flags[c] = fl;
       }
   return 0;
 }
 
-int orc_init_equilibrium_f32(const pog_params* p, const uint8_t* flags, float* f, float rho0,
+int orc_init_equilibrium_f32(const pog_params* p, const uint32_t* flags, float* f, float rho0,
                              float ux, float uy, float uz) {
   init_eq<float>(p, flags, f, rho0, ux, uy, uz);
   return 0;
 }
-int orc_init_equilibrium_f64(const pog_params* p, const uint8_t* flags, double* f, double rho0,
+int orc_init_equilibrium_f64(const pog_params* p, const uint32_t* flags, double* f, double rho0,
                              double ux, double uy, double uz) {
   init_eq<double>(p, flags, f, rho0, ux, uy, uz);
   return 0;
@@ -494,15 +519,16 @@ int orc_init_equilibrium_f64(const pog_params* p, const uint8_t* flags, double* 
 
 // One step, natural layout, f_out must be a different buffer.  u_prev: [3][n] velocity of the
 // previous step (LES stencil mode) or null.  Fe: [3][n] float external force or null.
-int orc_step_f32(const pog_params* p, const uint8_t* flags, const float* f, float* fo,
-                 const float* Fe, const float* eps, const float* u_prev, float* rho_out,
-                 float* u_out, double* red) {
-  return step_push<float>(p, flags, f, fo, Fe, eps, u_prev, rho_out, u_out, red);
+// Pd: [4][n] float particle drag deposit (Kp, Kv) or null.
+int orc_step_f32(const pog_params* p, const uint32_t* flags, const float* f, float* fo,
+                 const float* Fe, const float* Pd, const float* eps, const float* u_prev,
+                 float* rho_out, float* u_out, double* red) {
+  return step_push<float>(p, flags, f, fo, Fe, Pd, eps, u_prev, rho_out, u_out, red);
 }
-int orc_step_f64(const pog_params* p, const uint8_t* flags, const double* f, double* fo,
-                 const float* Fe, const float* eps, const double* u_prev, double* rho_out,
-                 double* u_out, double* red) {
-  return step_push<double>(p, flags, f, fo, Fe, eps, u_prev, rho_out, u_out, red);
+int orc_step_f64(const pog_params* p, const uint32_t* flags, const double* f, double* fo,
+                 const float* Fe, const float* Pd, const float* eps, const double* u_prev,
+                 double* rho_out, double* u_out, double* red) {
+  return step_push<double>(p, flags, f, fo, Fe, Pd, eps, u_prev, rho_out, u_out, red);
 }
 
 // ---- function-level helpers for the known-answer tests ------------------------------------
@@ -527,7 +553,7 @@ void orc_moments_f64(const double* f, double* rho, double* u) {
   u[2] = r > 1e-12 ? mz / r : 0;
 }
 // LES nu_sgs field from a [3][n] velocity (les_turbulence.py:318-380).
-int orc_les_nu_f32(const pog_params* p, const uint8_t* flags, const float* u, float* nu) {
+int orc_les_nu_f32(const pog_params* p, const uint32_t* flags, const float* u, float* nu) {
   Geo g = make_geo(p);
   for (int k = 0; k < g.nz; ++k)
     for (int j = 0; j < g.ny; ++j)
@@ -536,7 +562,7 @@ int orc_les_nu_f32(const pog_params* p, const uint8_t* flags, const float* u, fl
 }
 // Darcy-Forchheimer force density at a given rho/u in porous cells, the drag_mode form
 // (filter_paper.py:471-536).  F: [3][n]; zero outside the band.
-int orc_porous_force_f32(const pog_params* p, const uint8_t* flags, const float* rho,
+int orc_porous_force_f32(const pog_params* p, const uint32_t* flags, const float* rho,
                          const float* u, float* F) {
   Geo g = make_geo(p);
   const long long n = g.n;
@@ -629,7 +655,7 @@ inline Dual sqrt(const Dual& a) {
 }
 }  // namespace
 
-extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint8_t* flags, const double* ft,
+extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint32_t* flags, const double* ft,
                                     const double* lam_next, double* lam_t, const float* eps,
                                     double* grad_eps, double* grad_inlet) {
   Geo g = make_geo(p);
@@ -643,7 +669,7 @@ extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint8_t* flags, c
       for (int j = 0; j < g.ny; ++j)
         for (int i = 0; i < g.nx; ++i) {
           long long c = g.idx(i, j, k);
-          uint8_t fl = flags[c];
+          uint32_t fl = flags[c];
           if (fl & POG_CELL_SOLID) {
             for (int q = 0; q < 19; ++q) lam_t[q * n + c] = 0;
             continue;
@@ -665,8 +691,8 @@ extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint8_t* flags, c
             coef[kk] = Dual((double)p->inlet_coef[kk]);
             coef[kk].d[20 + kk] = 1.0;
           }
-          collide<Dual>(p, g, fl, i, j, k, f, nullptr, eps != nullptr, e, Dual(0.0), fs, rho, u,
-                        nullptr, coef);
+          collide<Dual>(p, g, fl, i, j, k, f, nullptr, nullptr, eps != nullptr, e, Dual(0.0), fs,
+                        rho, u, nullptr, coef);
           for (int q = 0; q < 19; ++q) {
             double acc = 0;
             for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[q];

@@ -7,10 +7,11 @@
 // 734-831) and the coupled-step order of LBMSolver.step_with_two_way_coupling
 // (legacy/lbm_solver.py:1485-1509), in lattice units, with the build-spec corrections:
 // Stokes drag in lattice units (the reference's magnitude misses a |u_rel| factor), the
-// relaxed force is both spread and integrated, and the particles are integrated in the
-// coupled step.  Every operation is a single IEEE float operation evaluated in the written
+// relaxed force is integrated, the particles are integrated in the coupled step, and the
+// fluid receives the drag implicitly: each particle deposits beta = m_p/(tau_p + dt) and
+// beta*v_new (Kp, Kv) on the 8 gather nodes and the lattice step applies Kv - Kp u.  Every operation is a single IEEE float operation evaluated in the written
 // order (compiled with -ffp-contract=off), so per-particle results are bit-identical with the
-// CUDA kernels, and the fixed-point force grid is bit-identical too.
+// CUDA kernels, and the fixed-point drag deposit is bit-identical too.
 //
 // Only tests/, smoke() and bench.py's CPU leg use this file.
 
@@ -113,8 +114,9 @@ void orc_under_relax(float a, const float* fnew, float* fold, float* fout, int m
   }
 }
 
-// One coupling pass over all particles (serial, in id order).  force_fix: [3][n] int64
-// accumulator (scale 2^32), added to.  u: [3][n] fluid velocity.  u_at (nullable): [3][np].
+// One coupling pass over all particles (serial, in id order).  force_fix: [4][n] int64
+// accumulator (scale 2^32) of the drag deposit (Kp, Kv_x, Kv_y, Kv_z), added to.  u: [3][n]
+// fluid velocity.  u_at (nullable): [3][np].
 int orc_particles_couple(const pog_params* p, const pog_particle_params* pp, float* pos,
                          float* vel, const float* diam, float* drag_old, int32_t* active, int np,
                          const float* u, long long* force_fix, float* u_at) {
@@ -175,18 +177,12 @@ int orc_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
       taup = taup / fac;
     }
     float gvec[3] = {p->gx, p->gy, p->gz};
+    float beta = mp / (taup + dt);  // drag coefficient: F_new = beta (u_f - v)
     float F[3];
     for (int a = 0; a < 3; ++a) {
       float fnew = mp * ur[a] / (taup + dt);
       F[a] = alpha * fnew + (1.0f - alpha) * drag_old[a * np + q];
       drag_old[a * np + q] = F[a];
-    }
-    for (int a = 0; a < 3; ++a) {
-      float mF = -F[a];
-      for (int c = 0; c < 8; ++c) {
-        float contrib = w[c] * mF;
-        force_fix[a * n + nodes[c]] += (long long)llrint((double)contrib * FIX_SCALE);
-      }
     }
     float nv[3], np3[3] = {x, y, z};
     for (int a = 0; a < 3; ++a) {
@@ -225,6 +221,14 @@ int orc_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
       pos[a * np + q] = np3[a];
       vel[a * np + q] = nv[a];
     }
+    // deposit Kp += w beta, Kv += w beta v_new on the 8 nodes of the gather position; the lattice
+    // step takes the particle force on the fluid, Kv - Kp u, implicitly
+    float dep[4] = {beta, beta * nv[0], beta * nv[1], beta * nv[2]};
+    for (int a = 0; a < 4; ++a)
+      for (int c = 0; c < 8; ++c) {
+        float contrib = w[c] * dep[a];
+        force_fix[a * n + nodes[c]] += (long long)llrint((double)contrib * FIX_SCALE);
+      }
   }
   return 0;
 }

@@ -30,15 +30,15 @@ SIGNATURES = [
     ("pog_validate_params", _i, [_P]),
     ("pog_build_flags", _i, [_P, _v, _v]),
     ("pog_init_equilibrium", _i, [_P, _v, _v, _f, _f, _f, _f, _v]),
-    ("pog_step", _i, [_P, _v, _v, _ll, _i, _v, _v, _v, _v, _v, _v, _v, _v]),
-    ("pog_step_push", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
+    ("pog_step", _i, [_P, _v, _v, _ll, _i, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
+    ("pog_step_push", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_export_natural", _i, [_P, _v, _v, _ll, _v, _i, _v]),
     ("pog_import_natural", _i, [_P, _v, _i, _v, _v, _v]),
-    ("pog_macroscopic", _i, [_P, _v, _v, _ll, _v, _v, _v, _v]),
+    ("pog_macroscopic", _i, [_P, _v, _v, _ll, _v, _v, _v, _v, _v]),
     ("pog_particles_bin_scratch_bytes", ctypes.c_size_t, [_i]),
     ("pog_particles_bin", _i, [_P, _v, _v, _i, _v, _v, _v, _v]),
     ("pog_particles_couple", _i, [_P, _PP, _v, _v, _v, _v, _v, _i, _v, _v, _v, _v, _v, _v]),
-    ("pog_force_from_fixed", _i, [_P, _v, _v, _v]),
+    ("pog_drag_from_fixed", _i, [_P, _v, _v, _v]),
     ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_device_status", _i, [_i]),
     ("pog_particles_bin_noalloc", _i, [_P, _v, _v, _i, _v, _v, _v]),

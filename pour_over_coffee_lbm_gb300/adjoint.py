@@ -43,7 +43,7 @@ class OutflowAdjoint:
         self.device = torch.device(device)
         shape = (cfg.nz, cfg.ny, cfg.nx)
         self.shape = shape
-        self.flags = torch.empty(shape, dtype=torch.uint8, device=self.device)
+        self.flags = torch.empty(shape, dtype=torch.int32, device=self.device)
         _lib.check(self.lib.pog_build_flags(cfg.to_c(), _lib.ptr(self.flags), _lib.stream_handle()))
         self.dtype = _DT[cfg.storage]
         self.nseg = (self.T + self.K - 1) // self.K
@@ -61,7 +61,7 @@ class OutflowAdjoint:
 
     def _push(self, fin, fout, red=None):
         _lib.check(self.lib.pog_step_push(self._p, _lib.ptr(fin), _lib.ptr(fout), _lib.ptr(self.flags),
-                                          None, _lib.ptr(self._eps), None, None, None,
+                                          None, None, _lib.ptr(self._eps), None, None, None,
                                           _lib.ptr(red), _lib.stream_handle()))
 
     def forward(self, porosity: Optional[torch.Tensor], inlet_coef) -> float:

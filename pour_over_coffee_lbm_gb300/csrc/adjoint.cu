@@ -67,7 +67,7 @@ template <int S>
 __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
-    const uint8_t* __restrict__ flags, const float* __restrict__ eps,
+    const uint32_t* __restrict__ flags, const float* __restrict__ eps,
     double* __restrict__ grad_eps, double* __restrict__ grad_inlet) {
   using St = Store<S>;
   using C = typename St::C;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
 #pragma unroll
   for (int k = 0; k < POG_INLET_NCOEF; ++k) ginl[k] = 0.0;
   for (uint32_t c = blockIdx.x * ADJ_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_BLOCK) {
-    const uint8_t fl = flags[c];
+    const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)0;
@@ -85,11 +85,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
     }
     // 1. transpose of push streaming
     C ls[19];
-    const bool near = (fl & POG_CELL_NEAR_SOLID) != 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
       const uint32_t dst = c + (uint32_t)kp.off[q];
-      const bool wall = near && q != 0 && (flags[dst] & POG_CELL_SOLID);
+      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
       ls[q] = wall ? (C)lam_next[(uint32_t)opp(q) * n + c] : (C)lam_next[(uint32_t)q * n + dst];
     }
     C f[19];
@@ -355,7 +354,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
 }
 
 template <int S>
-static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* lt, const uint8_t* flags,
+static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* lt, const uint32_t* flags,
                       const float* eps, double* ge, double* gi, cudaStream_t s) {
   auto kern = adjoint_kernel<S>;
   static thread_local int grid = 0;
@@ -375,7 +374,7 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
 using namespace pog;
 
 extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next,
-                                void* lam_t, const uint8_t* flags, const float* porosity,
+                                void* lam_t, const uint32_t* flags, const float* porosity,
                                 double* grad_porosity, double* grad_inlet, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;

@@ -77,9 +77,12 @@ __host__ __device__ __forceinline__ void collide_pair(C f[19], C ux, C uy, C uz,
 
 // f[19]: incoming populations on entry, post-collision populations on exit.
 // nu_st: nu_sgs from the velocity stencil (LES_STENCIL mode), computed by the caller.
+// pdrag: [4][n] particle drag deposit (Kp = sum w beta, Kv = sum w beta v_p) or null; the
+// particle force on the fluid, Kv - Kp u, is taken implicitly in u (stable at any loading).
 template <typename C>
-__host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint8_t fl, uint32_t c,
+__host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint32_t fl, uint32_t c,
                                                                C f[19], const float* __restrict__ force,
+                                                               const float* __restrict__ pdrag,
                                                                const float* __restrict__ eps, C nu_st) {
   CellResult<C> res;
   // ---- moments from one sweep of adds -------------------------------------------------------
@@ -124,8 +127,18 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     Gz += (C)force[2u * kp.n + c];
   }
   const C inv_rho = (C)1 / rho;
-  C ux = (mx + (C)0.5 * Gx) * inv_rho, uy = (my + (C)0.5 * Gy) * inv_rho,
-    uz = (mz + (C)0.5 * Gz) * inv_rho;
+  // Particle drag deposit: F_p = Kv - Kp u with u implicit.  v is the velocity with every
+  // explicit force, A the implicit factor (1 without particles).
+  C Kp = (C)0, Kvx = (C)0, Kvy = (C)0, Kvz = (C)0;
+  if (pdrag) {
+    Kp = (C)pdrag[c];
+    Kvx = (C)pdrag[kp.n + c];
+    Kvy = (C)pdrag[2u * kp.n + c];
+    Kvz = (C)pdrag[3u * kp.n + c];
+  }
+  const C A = (C)1 + (C)0.5 * Kp * inv_rho;
+  C ux = (mx + (C)0.5 * (Gx + Kvx)) * inv_rho, uy = (my + (C)0.5 * (Gy + Kvy)) * inv_rho,
+    uz = (mz + (C)0.5 * (Gz + Kvz)) * inv_rho;
   C Fx = Gx, Fy = Gy, Fz = Gz;
   const bool porous = (fl & POG_CELL_POROUS) != 0;
   if (porous) {
@@ -140,8 +153,8 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     C sK = sqrt(K);
     C nu0 = (C)kp.nu0;
     if (kp.drag_mode == POG_DRAG_SEMI_IMPLICIT) {
-      // Guo & Zhao 2002: u (1 + nu/(2K) + C_F|u|/(2 sqrt K)) = v, solved in closed form.
-      C c0 = (C)0.5 * ((C)1 + (C)0.5 * nu0 / K);
+      // Guo & Zhao 2002: u (A + nu/(2K) + C_F|u|/(2 sqrt K)) = v, solved in closed form.
+      C c0 = (C)0.5 * (A + (C)0.5 * nu0 / K);
       C c1 = (C)0.5 * CF / sK;
       C vm = sqrt(ux * ux + uy * uy + uz * uz);
       C s = (C)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
@@ -149,11 +162,14 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
       uy *= s;
       uz *= s;
       C um = sqrt(ux * ux + uy * uy + uz * uz);
-      C coef = rho * (nu0 / K + CF / sK * um);
-      Fx = Gx - coef * ux;
-      Fy = Gy - coef * uy;
-      Fz = Gz - coef * uz;
+      C coef = rho * (nu0 / K + CF / sK * um) + Kp;
+      Fx = Gx + Kvx - coef * ux;
+      Fy = Gy + Kvy - coef * uy;
+      Fz = Gz + Kvz - coef * uz;
     } else {
+      ux /= A;
+      uy /= A;
+      uz /= A;
       C vm = sqrt(ux * ux + uy * uy + uz * uz);
       C coef = rho * (nu0 / K + CF / sK * vm);
       C dx = -coef * ux, dy = -coef * uy, dz = -coef * uz;
@@ -165,13 +181,21 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
         dy *= sc;
         dz *= sc;
       }
-      Fx = Gx + dx;
-      Fy = Gy + dy;
-      Fz = Gz + dz;
-      ux = (mx + (C)0.5 * Fx) * inv_rho;
-      uy = (my + (C)0.5 * Fy) * inv_rho;
-      uz = (mz + (C)0.5 * Fz) * inv_rho;
+      // capped drag as an explicit force, particle drag implicit: u A = (m + (G + Kv + F_d)/2)/rho
+      ux = (mx + (C)0.5 * (Gx + Kvx + dx)) * inv_rho / A;
+      uy = (my + (C)0.5 * (Gy + Kvy + dy)) * inv_rho / A;
+      uz = (mz + (C)0.5 * (Gz + Kvz + dz)) * inv_rho / A;
+      Fx = Gx + dx + Kvx - Kp * ux;
+      Fy = Gy + dy + Kvy - Kp * uy;
+      Fz = Gz + dz + Kvz - Kp * uz;
     }
+  } else if (pdrag) {
+    ux /= A;
+    uy /= A;
+    uz /= A;
+    Fx = Gx + Kvx - Kp * ux;
+    Fy = Gy + Kvy - Kp * uy;
+    Fz = Gz + Kvz - Kp * uz;
   }
   const C usq = ux * ux + uy * uy + uz * uz;
   const C tau0 = (C)kp.tau;

@@ -21,7 +21,7 @@ __device__ inline double radius_at(const GeoParams& g, int i, int j) {
   return sqrt(dx * dx + dy * dy);
 }
 
-__global__ void solid_kernel(GeoParams g, uint8_t* flags) {
+__global__ void solid_kernel(GeoParams g, uint32_t* flags) {
   long long n = (long long)g.nx * g.ny * g.nz;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x) {
@@ -41,7 +41,7 @@ __global__ void solid_kernel(GeoParams g, uint8_t* flags) {
   }
 }
 
-__global__ void fluid_bits_kernel(GeoParams g, uint8_t* flags) {
+__global__ void fluid_bits_kernel(GeoParams g, uint32_t* flags) {
   long long n = (long long)g.nx * g.ny * g.nz;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x) {
@@ -52,20 +52,20 @@ __global__ void fluid_bits_kernel(GeoParams g, uint8_t* flags) {
     double r = radius_at(g, i, j);
     double z = (double)k;
     double rc = (z - g.apex) * g.tanth;
-    uint8_t fl = 0;
+    uint32_t fl = 0;
     if (k == g.nz - 2 && r <= g.rin) fl |= POG_CELL_INLET;
     if (k == 1 && r <= g.hole) fl |= POG_CELL_OUTLET;
     if (!(fl & (POG_CELL_INLET | POG_CELL_OUTLET)) && g.band > 0 && z >= g.apex &&
         r > rc - g.band && r <= rc + g.wall)
       fl |= POG_CELL_POROUS;
     // Fluid cells are never on the outer shell, so every neighbour is in the grid.
-    bool near = false;
+    uint32_t links = 0;
 #pragma unroll
     for (int q = 1; q < 19; ++q) {
       long long nb = c + cx(q) + (long long)cy(q) * g.nx + (long long)cz(q) * g.nx * g.ny;
-      near = near || (flags[nb] & POG_CELL_SOLID);
+      if (flags[nb] & POG_CELL_SOLID) links |= 1u << (POG_LINK_SHIFT + q);
     }
-    if (near) fl |= POG_CELL_NEAR_SOLID;
+    if (links) fl |= POG_CELL_NEAR_SOLID | links;
     flags[c] = fl;
   }
 }
@@ -74,7 +74,7 @@ __global__ void fluid_bits_kernel(GeoParams g, uint8_t* flags) {
 
 using namespace pog;
 
-extern "C" int pog_build_flags(const pog_params* p, uint8_t* flags, void* stream) {
+extern "C" int pog_build_flags(const pog_params* p, uint32_t* flags, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
   if (!flags) return set_error(POG_E_ARG, "flags is NULL");

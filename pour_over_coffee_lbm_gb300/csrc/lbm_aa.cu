@@ -33,8 +33,8 @@ constexpr int AA_BLOCK = 256;
 
 template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
 __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
-    const KParams kp, typename Store<S>::E* __restrict__ f, const uint8_t* __restrict__ flags,
-    const float* __restrict__ force, const float* __restrict__ eps,
+    const KParams kp, typename Store<S>::E* __restrict__ f, const uint32_t* __restrict__ flags,
+    const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
     const float* __restrict__ u_prev, float* __restrict__ u_next, float* __restrict__ rho_out,
     float* __restrict__ u_out, double* __restrict__ red) {
   using St = Store<S>;
@@ -47,30 +47,25 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
     for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] = 0.0;
   }
   for (uint32_t c = blockIdx.x * AA_BLOCK + threadIdx.x; c < n; c += gridDim.x * AA_BLOCK) {
-    const uint8_t fl = flags[c];
+    const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
-    const bool near = (fl & POG_CELL_NEAR_SOLID) != 0;
     C fv[19];
     if (PARITY == 0) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) fv[q] = St::ld(f, (uint32_t)q * n + c, q, rho0);
-    } else if (!near) {
-#pragma unroll
-      for (int q = 0; q < 19; ++q)
-        fv[q] = St::ld(f, (uint32_t)opp(q) * n + (c - (uint32_t)kp.off[q]), opp(q), rho0);
     } else {
+      // source c - e_q is the neighbour in direction opp(q); a solid one bounces f_q back
 #pragma unroll
       for (int q = 0; q < 19; ++q) {
-        const uint32_t src = c - (uint32_t)kp.off[q];
-        const bool wall = q != 0 && (flags[src] & POG_CELL_SOLID);
-        fv[q] = wall ? St::ld(f, (uint32_t)q * n + c, q, rho0)
-                     : St::ld(f, (uint32_t)opp(q) * n + src, opp(q), rho0);
+        const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
+        const uint32_t idx = wall ? (uint32_t)q * n + c : (uint32_t)opp(q) * n + (c - (uint32_t)kp.off[q]);
+        fv[q] = St::ld(f, idx, q, rho0);
       }
     }
     C nu_st = (C)0;
     if (!MACRO_ONLY && kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS))
       nu_st = les_nu_stencil<C>(kp, c, u_prev);
-    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, eps, nu_st);
+    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, pdrag, eps, nu_st);
     if (rho_out) rho_out[c] = (float)r.rho;
     if (u_out) {
       u_out[c] = (float)r.ux;
@@ -96,18 +91,12 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
     if (PARITY == 0) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) St::st(f, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
-    } else if (!near) {
-#pragma unroll
-      for (int q = 0; q < 19; ++q) St::st(f, (uint32_t)q * n + (c + (uint32_t)kp.off[q]), q, fv[q], rho0);
     } else {
 #pragma unroll
       for (int q = 0; q < 19; ++q) {
-        const uint32_t dst = c + (uint32_t)kp.off[q];
-        const bool wall = q != 0 && (flags[dst] & POG_CELL_SOLID);
-        if (wall)
-          St::st(f, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
-        else
-          St::st(f, (uint32_t)q * n + dst, q, fv[q], rho0);
+        const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
+        const uint32_t idx = wall ? (uint32_t)opp(q) * n + c : (uint32_t)q * n + (c + (uint32_t)kp.off[q]);
+        St::st(f, idx, q, fv[q], rho0);
       }
     }
   }
@@ -117,13 +106,13 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
 // Natural-layout copy of the AA state at parity PARITY (odd = the odd-step read gather).
 template <int S, int PARITY, typename O>
 __global__ void aa_export_kernel(const KParams kp, const typename Store<S>::E* __restrict__ f,
-                                 const uint8_t* __restrict__ flags, O* __restrict__ out) {
+                                 const uint32_t* __restrict__ flags, O* __restrict__ out) {
   using St = Store<S>;
   using C = typename St::C;
   const C rho0 = (C)kp.rho0;
   const uint32_t n = kp.n;
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-    const uint8_t fl = flags[c];
+    const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) out[(size_t)q * n + c] = (O)0;
@@ -135,10 +124,9 @@ __global__ void aa_export_kernel(const KParams kp, const typename Store<S>::E* _
       if (PARITY == 0) {
         v = St::ld(f, (uint32_t)q * n + c, q, rho0);
       } else {
-        const uint32_t src = c - (uint32_t)kp.off[q];
-        const bool wall = q != 0 && (flags[src] & POG_CELL_SOLID);
+        const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
         v = wall ? St::ld(f, (uint32_t)q * n + c, q, rho0)
-                 : St::ld(f, (uint32_t)opp(q) * n + src, opp(q), rho0);
+                 : St::ld(f, (uint32_t)opp(q) * n + (c - (uint32_t)kp.off[q]), opp(q), rho0);
       }
       out[(size_t)q * n + c] = (O)v;
     }
@@ -147,7 +135,7 @@ __global__ void aa_export_kernel(const KParams kp, const typename Store<S>::E* _
 
 template <int S, typename I>
 __global__ void aa_import_kernel(const KParams kp, const I* __restrict__ in,
-                                 const uint8_t* __restrict__ flags, typename Store<S>::E* __restrict__ f) {
+                                 const uint32_t* __restrict__ flags, typename Store<S>::E* __restrict__ f) {
   using St = Store<S>;
   using C = typename St::C;
   const C rho0 = (C)kp.rho0;
@@ -164,7 +152,7 @@ __global__ void aa_import_kernel(const KParams kp, const I* __restrict__ in,
 
 template <int S>
 __global__ void aa_init_kernel(const KParams kp, typename Store<S>::E* __restrict__ f,
-                               const uint8_t* __restrict__ flags, float rho, float ux, float uy,
+                               const uint32_t* __restrict__ flags, float rho, float ux, float uy,
                                float uz) {
   using St = Store<S>;
   using C = typename St::C;
@@ -183,8 +171,8 @@ __global__ void aa_init_kernel(const KParams kp, typename Store<S>::E* __restric
 
 // ---- host dispatch ----------------------------------------------------------------------------
 template <int S, int PARITY, bool REDUCE, bool MACRO>
-static int launch_aa(const KParams& kp, void* f, const uint8_t* flags, const float* force,
-                     const float* eps, const float* u_prev, float* u_next, float* rho_out,
+static int launch_aa(const KParams& kp, void* f, const uint32_t* flags, const float* force,
+                     const float* pdrag, const float* eps, const float* u_prev, float* u_next, float* rho_out,
                      float* u_out, double* red, cudaStream_t s) {
   auto kern = aa_step_kernel<S, PARITY, REDUCE, MACRO>;
   static thread_local int grid = 0;
@@ -192,7 +180,7 @@ static int launch_aa(const KParams& kp, void* f, const uint8_t* flags, const flo
   if (grid <= 0) return set_error(POG_E_CUDA, "occupancy query failed");
   int want = (int)((kp.n + AA_BLOCK - 1) / AA_BLOCK);
   int g = (POG_AA_ONE_CELL && !REDUCE) ? want : (want < grid ? want : grid);
-  kern<<<g, AA_BLOCK, 0, s>>>(kp, (typename Store<S>::E*)f, flags, force, eps, u_prev, u_next,
+  kern<<<g, AA_BLOCK, 0, s>>>(kp, (typename Store<S>::E*)f, flags, force, pdrag, eps, u_prev, u_next,
                               rho_out, u_out, red);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
@@ -201,12 +189,12 @@ static int launch_aa(const KParams& kp, void* f, const uint8_t* flags, const flo
 
 template <int S>
 static int dispatch_aa(const KParams& kp, int parity, bool reduce, bool macro, void* f,
-                       const uint8_t* flags, const float* force, const float* eps,
+                       const uint32_t* flags, const float* force, const float* pdrag, const float* eps,
                        const float* u_prev, float* u_next, float* rho_out, float* u_out,
                        double* red, cudaStream_t s) {
 #define POG_AA_CASE(P, R, M)                                                                    \
   if (parity == P && reduce == R && macro == M)                                                 \
-    return launch_aa<S, P, R, M>(kp, f, flags, force, eps, u_prev, u_next, rho_out, u_out, red, s);
+    return launch_aa<S, P, R, M>(kp, f, flags, force, pdrag, eps, u_prev, u_next, rho_out, u_out, red, s);
   POG_AA_CASE(0, false, false)
   POG_AA_CASE(1, false, false)
   POG_AA_CASE(0, true, false)
@@ -218,33 +206,34 @@ static int dispatch_aa(const KParams& kp, int parity, bool reduce, bool macro, v
 }
 
 static int dispatch_storage(const KParams& kp, int parity, bool reduce, bool macro, void* f,
-                            const uint8_t* flags, const float* force, const float* eps,
+                            const uint32_t* flags, const float* force, const float* pdrag, const float* eps,
                             const float* u_prev, float* u_next, float* rho_out, float* u_out,
                             double* red, cudaStream_t s) {
   switch (kp.storage) {
     case POG_STORE_F32:
-      return dispatch_aa<POG_STORE_F32>(kp, parity, reduce, macro, f, flags, force, eps, u_prev, u_next, rho_out, u_out, red, s);
+      return dispatch_aa<POG_STORE_F32>(kp, parity, reduce, macro, f, flags, force, pdrag, eps, u_prev, u_next, rho_out, u_out, red, s);
     case POG_STORE_F16S:
-      return dispatch_aa<POG_STORE_F16S>(kp, parity, reduce, macro, f, flags, force, eps, u_prev, u_next, rho_out, u_out, red, s);
+      return dispatch_aa<POG_STORE_F16S>(kp, parity, reduce, macro, f, flags, force, pdrag, eps, u_prev, u_next, rho_out, u_out, red, s);
     case POG_STORE_BF16S:
-      return dispatch_aa<POG_STORE_BF16S>(kp, parity, reduce, macro, f, flags, force, eps, u_prev, u_next, rho_out, u_out, red, s);
+      return dispatch_aa<POG_STORE_BF16S>(kp, parity, reduce, macro, f, flags, force, pdrag, eps, u_prev, u_next, rho_out, u_out, red, s);
     case POG_STORE_F64:
-      return dispatch_aa<POG_STORE_F64>(kp, parity, reduce, macro, f, flags, force, eps, u_prev, u_next, rho_out, u_out, red, s);
+      return dispatch_aa<POG_STORE_F64>(kp, parity, reduce, macro, f, flags, force, pdrag, eps, u_prev, u_next, rho_out, u_out, red, s);
   }
   return set_error(POG_E_ARG, "storage %d unknown", kp.storage);
 }
 
-int launch_aa_tma(const KParams& kp, int parity, bool reduce, void* f, const uint8_t* flags,
-                  const float* force, const float* eps, const float* u_prev, float* u_next,
+int launch_aa_tma(const KParams& kp, int parity, bool reduce, void* f, const uint32_t* flags,
+                  const float* force, const float* pdrag, const float* eps, const float* u_prev, float* u_next,
                   float* rho_out, float* u_out, double* red, cudaStream_t s);
 
-// Which step kernel pog_step uses: the TMA-staged one (default; needs a 16-byte aligned
-// distribution buffer) or the register-staged one (POG_AA_KERNEL=plain, kept for A/B timing).
+// Which step kernel pog_step uses: the register-staged one (default: measured faster on GB300
+// once bounce-back needs no neighbour loads) or the TMA-staged one (POG_AA_KERNEL=tma, needs a
+// 16-byte aligned distribution buffer; kept for A/B timing).
 static bool use_tma(const void* f) {
   static int mode = -1;
   if (mode < 0) {
     const char* e = getenv("POG_AA_KERNEL");
-    mode = (e && e[0] == 'p') ? 0 : 1;
+    mode = (e && e[0] == 't') ? 1 : 0;
   }
   return mode == 1 && ((uintptr_t)f & 15u) == 0;
 }
@@ -271,7 +260,7 @@ using namespace pog;
 
 extern "C" {
 
-int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, float rho0, float ux,
+int pog_init_equilibrium(const pog_params* p, void* f, const uint32_t* flags, float rho0, float ux,
                          float uy, float uz, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
@@ -290,8 +279,8 @@ int pog_init_equilibrium(const pog_params* p, void* f, const uint8_t* flags, flo
   return POG_OK;
 }
 
-int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, int nsteps,
-             const float* force, const float* porosity, float* u_prev, float* u_next,
+int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, int nsteps,
+             const float* force, const float* pdrag, const float* porosity, float* u_prev, float* u_next,
              float* rho_out, float* u_out, double* reductions, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
@@ -311,11 +300,11 @@ int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, in
     const bool last = i == nsteps - 1;
     const int parity = (int)((t + i) & 1);
     if (use_tma(f))
-      rc = launch_aa_tma(kp, parity, reductions != nullptr, f, flags, force, porosity,
+      rc = launch_aa_tma(kp, parity, reductions != nullptr, f, flags, force, pdrag, porosity,
                          stencil ? up : nullptr, stencil ? un : nullptr, last ? rho_out : nullptr,
                          last ? u_out : nullptr, reductions, s);
     else
-      rc = dispatch_storage(kp, parity, reductions != nullptr, false, f, flags, force, porosity,
+      rc = dispatch_storage(kp, parity, reductions != nullptr, false, f, flags, force, pdrag, porosity,
                             stencil ? up : nullptr, stencil ? un : nullptr,
                             last ? rho_out : nullptr, last ? u_out : nullptr,
                             reductions, s);
@@ -329,18 +318,18 @@ int pog_step(const pog_params* p, void* f, const uint8_t* flags, long long t, in
   return POG_OK;
 }
 
-int pog_macroscopic(const pog_params* p, const void* f, const uint8_t* flags, long long t,
-                    const float* force, float* rho_out, float* u_out, void* stream) {
+int pog_macroscopic(const pog_params* p, const void* f, const uint32_t* flags, long long t,
+                    const float* force, const float* pdrag, float* rho_out, float* u_out, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
   if (!f || !flags) return set_error(POG_E_ARG, "f/flags is NULL");
   KParams kp = make_kparams(p);
   if (kp.les_mode == POG_LES_STENCIL) kp.les_mode = POG_LES_OFF;  // u does not depend on tau
-  return dispatch_storage(kp, (int)(t & 1), false, true, (void*)f, flags, force, nullptr, nullptr,
+  return dispatch_storage(kp, (int)(t & 1), false, true, (void*)f, flags, force, pdrag, nullptr, nullptr,
                           nullptr, rho_out, u_out, nullptr, (cudaStream_t)stream);
 }
 
-int pog_export_natural(const pog_params* p, const void* f, const uint8_t* flags, long long t,
+int pog_export_natural(const pog_params* p, const void* f, const uint32_t* flags, long long t,
                        void* f_nat, int out_storage, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
@@ -371,7 +360,7 @@ int pog_export_natural(const pog_params* p, const void* f, const uint8_t* flags,
   return POG_OK;
 }
 
-int pog_import_natural(const pog_params* p, const void* f_nat, int in_storage, const uint8_t* flags,
+int pog_import_natural(const pog_params* p, const void* f_nat, int in_storage, const uint32_t* flags,
                        void* f, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;

@@ -11,8 +11,8 @@ constexpr int PUSH_BLOCK = 256;
 template <int S, bool REDUCE>
 __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ fin,
-    typename Store<S>::E* __restrict__ fout, const uint8_t* __restrict__ flags,
-    const float* __restrict__ force, const float* __restrict__ eps,
+    typename Store<S>::E* __restrict__ fout, const uint32_t* __restrict__ flags,
+    const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
     const float* __restrict__ u_prev, float* __restrict__ rho_out, float* __restrict__ u_out,
     double* __restrict__ red) {
   using St = Store<S>;
@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
     for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] = 0.0;
   }
   for (uint32_t c = blockIdx.x * PUSH_BLOCK + threadIdx.x; c < n; c += gridDim.x * PUSH_BLOCK) {
-    const uint8_t fl = flags[c];
+    const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
     C fv[19];
 #pragma unroll
@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
     C nu_st = (C)0;
     if (kp.les_mode == POG_LES_STENCIL && u_prev && !(fl & POG_CELL_POROUS))
       nu_st = les_nu_stencil<C>(kp, c, u_prev);
-    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, eps, nu_st);
+    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, pdrag, eps, nu_st);
     if (rho_out) rho_out[c] = (float)r.rho;
     if (u_out) {
       u_out[c] = (float)r.ux;
@@ -50,11 +50,10 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
                          isfinite((double)r.uy) && isfinite((double)r.uz));
       acc[POG_RED_NONFINITE] += bad ? 1.0 : 0.0;
     }
-    const bool near = (fl & POG_CELL_NEAR_SOLID) != 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
       const uint32_t dst = c + (uint32_t)kp.off[q];
-      const bool wall = near && q != 0 && (flags[dst] & POG_CELL_SOLID);
+      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
       if (wall)
         St::st(fout, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
       else
@@ -65,8 +64,8 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
 }
 
 template <int S, bool R>
-static int launch_push(const KParams& kp, const void* fin, void* fout, const uint8_t* flags,
-                       const float* force, const float* eps, const float* u_prev, float* rho_out,
+static int launch_push(const KParams& kp, const void* fin, void* fout, const uint32_t* flags,
+                       const float* force, const float* pdrag, const float* eps, const float* u_prev, float* rho_out,
                        float* u_out, double* red, cudaStream_t s) {
   auto kern = push_step_kernel<S, R>;
   static thread_local int grid = 0;
@@ -75,7 +74,7 @@ static int launch_push(const KParams& kp, const void* fin, void* fout, const uin
   int want = (int)((kp.n + PUSH_BLOCK - 1) / PUSH_BLOCK);
   int g = want < grid ? want : grid;
   using E = typename Store<S>::E;
-  kern<<<g, PUSH_BLOCK, 0, s>>>(kp, (const E*)fin, (E*)fout, flags, force, eps, u_prev, rho_out,
+  kern<<<g, PUSH_BLOCK, 0, s>>>(kp, (const E*)fin, (E*)fout, flags, force, pdrag, eps, u_prev, rho_out,
                                 u_out, red);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
@@ -87,7 +86,8 @@ static int launch_push(const KParams& kp, const void* fin, void* fout, const uin
 using namespace pog;
 
 extern "C" int pog_step_push(const pog_params* p, const void* f_in, void* f_out,
-                             const uint8_t* flags, const float* force, const float* porosity,
+                             const uint32_t* flags, const float* force, const float* pdrag,
+                             const float* porosity,
                              const float* u_prev, float* rho_out, float* u_out,
                              double* reductions, void* stream) {
   int rc = pog_validate_params(p);
@@ -101,8 +101,8 @@ extern "C" int pog_step_push(const pog_params* p, const void* f_in, void* f_out,
   const bool R = reductions != nullptr;
 #define POG_PUSH(SS)                                                                              \
   if (p->storage == SS)                                                                           \
-    return R ? launch_push<SS, true>(kp, f_in, f_out, flags, force, porosity, u_prev, rho_out, u_out, reductions, s) \
-             : launch_push<SS, false>(kp, f_in, f_out, flags, force, porosity, u_prev, rho_out, u_out, reductions, s);
+    return R ? launch_push<SS, true>(kp, f_in, f_out, flags, force, pdrag, porosity, u_prev, rho_out, u_out, reductions, s) \
+             : launch_push<SS, false>(kp, f_in, f_out, flags, force, pdrag, porosity, u_prev, rho_out, u_out, reductions, s);
   POG_PUSH(POG_STORE_F32)
   POG_PUSH(POG_STORE_F16S)
   POG_PUSH(POG_STORE_BF16S)

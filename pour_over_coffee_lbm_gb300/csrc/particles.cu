@@ -5,11 +5,15 @@
 // compute_drag_coefficient 1088-1099, compute_two_way_coupling_forces 1107-1154,
 // apply_under_relaxation 1200-1212, update_particle_physics 641-720 (+ cone constraint
 // 734-831), in the order of LBMSolver.step_with_two_way_coupling (legacy/lbm_solver.py:
-// 1485-1509).  The reference spreads with one ti.atomic_add per node and particle; here
-// particles are processed in cell order (a stable LSD radix sort on the cell key) and lanes
-// of a warp that hit the same node combine their contributions with a segmented warp
-// reduction before one atomic per node ("warp-aggregated atomics").  A deterministic mode
-// accumulates 2^32-scaled int64 fixed point instead, which is order-independent.
+// 1485-1509).  The fluid side: the reference spreads the explicit reaction -F onto the 8 nodes;
+// here each particle deposits its drag coefficient beta = m_p/(tau_p + dt) and beta*v onto
+// them (Kp, Kv) and the lattice step applies the particle force Kv - Kp u implicitly in u,
+// which stays stable where the flow packs particles into a few cells (the explicit exchange
+// diverges once a cell's particle mass exceeds its fluid mass).  Particles are processed in
+// cell order (a stable LSD radix sort on the cell key) and lanes of a warp that hit the same
+// node combine their contributions with a segmented warp reduction before one atomic per node
+// ("warp-aggregated atomics").  A deterministic mode accumulates 2^32-scaled int64 fixed point
+// instead, which is order-independent.
 //
 // This translation unit is compiled with -fmad=false: every float operation is a single
 // IEEE operation in the written order, so per-particle results are bit-identical with the
@@ -208,8 +212,8 @@ __device__ __forceinline__ void warp_aggregated_add(float* base, uint32_t node, 
 __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __restrict__ vel,
                               const float* __restrict__ diam, float* __restrict__ drag_old,
                               int32_t* __restrict__ active, int np, const int32_t* __restrict__ order,
-                              const float* __restrict__ u, float* __restrict__ force,
-                              unsigned long long* __restrict__ force_fix,
+                              const float* __restrict__ u, float* __restrict__ pdrag,
+                              unsigned long long* __restrict__ pdrag_fix,
                               float* __restrict__ u_at) {
   const float PI_F = 3.14159265358979f;
   const uint32_t n = P.n;
@@ -224,6 +228,8 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
     int i = 0, j = 0, k = 0;
     float w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     float F[3] = {0, 0, 0};
+    float dep[4] = {0, 0, 0, 0};  // deposit: beta, beta * v_new
+    bool dep_ok = false;
     if (ok) {
       x = pos[q];
       y = pos[np + q];
@@ -279,6 +285,7 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
         taup = taup / fac;
       }
       const float gv[3] = {P.gx, P.gy, P.gz};
+      const float beta = mp / (taup + P.dt);  // drag coefficient: F_new = beta (u_f - v)
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         float fnew = mp * ur[a] / (taup + P.dt);
@@ -325,22 +332,27 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
           pos[a * np + q] = np3[a];
           vel[a * np + q] = nv[a];
         }
+        dep[0] = beta;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) dep[1 + a] = beta * nv[a];
+        dep_ok = true;
       }
     }
-    // spread -F (the relaxed drag) with the gather weights at the pre-update position
+    // Deposit the drag coefficient and its momentum weight (Kp += w beta, Kv += w beta v_new)
+    // with the gather weights at the pre-update position; the lattice step applies the
+    // particle force on the fluid, Kv - Kp u, implicitly in u.
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float mF = -F[a];
+    for (int a = 0; a < 4; ++a) {
 #pragma unroll
       for (int cc = 0; cc < 8; ++cc) {
-        const float contrib = w[cc] * mF;
+        const float contrib = w[cc] * dep[a];
         if (P.deterministic) {
-          if (ok) {
+          if (dep_ok) {
             long long fixv = __double2ll_rn((double)contrib * FIX_SCALE);
-            atomicAdd(force_fix + (size_t)a * n + nodes[cc], (unsigned long long)fixv);
+            atomicAdd(pdrag_fix + (size_t)a * n + nodes[cc], (unsigned long long)fixv);
           }
         } else {
-          warp_aggregated_add(force + (size_t)a * n, nodes[cc], ok, contrib);
+          warp_aggregated_add(pdrag + (size_t)a * n, nodes[cc], dep_ok, contrib);
         }
       }
     }
@@ -437,7 +449,7 @@ int pog_particles_bin(const pog_params* p, const float* pos, const int32_t* acti
 
 int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, float* pos, float* vel,
                          const float* diameter, float* drag_old, int32_t* active, int np,
-                         const int32_t* order, const float* u, float* force, long long* force_fix,
+                         const int32_t* order, const float* u, float* pdrag, long long* pdrag_fix,
                          float* u_at_particle, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
@@ -446,8 +458,8 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   if (np == 0) return POG_OK;
   if (!pos || !vel || !diameter || !drag_old || !active || !u)
     return set_error(POG_E_ARG, "a particle array or u is NULL");
-  if (pp->deterministic ? !force_fix : !force)
-    return set_error(POG_E_ARG, "force accumulator for the selected mode is NULL");
+  if (pp->deterministic ? !pdrag_fix : !pdrag)
+    return set_error(POG_E_ARG, "drag accumulator for the selected mode is NULL");
   PKParams P;
   P.nx = p->nx;
   P.ny = p->ny;
@@ -477,21 +489,21 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   int block = 256;
   int grid = (np + block - 1) / block;
   if (grid > 152 * 16) grid = 152 * 16;
-  couple_kernel<<<grid, block, 0, s>>>(P, pos, vel, diameter, drag_old, active, np, order, u, force,
-                                       (unsigned long long*)force_fix, u_at_particle);
+  couple_kernel<<<grid, block, 0, s>>>(P, pos, vel, diameter, drag_old, active, np, order, u, pdrag,
+                                       (unsigned long long*)pdrag_fix, u_at_particle);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;
 }
 
-int pog_force_from_fixed(const pog_params* p, const long long* force_fix, float* force, void* stream) {
+int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* pdrag, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
-  if (!force_fix || !force) return set_error(POG_E_ARG, "NULL pointer");
-  uint32_t n3 = 3u * (uint32_t)p->nx * p->ny * p->nz;
+  if (!pdrag_fix || !pdrag) return set_error(POG_E_ARG, "NULL pointer");
+  uint32_t n3 = 4u * (uint32_t)p->nx * p->ny * p->nz;
   int grid = (int)((n3 + 255) / 256);
   if (grid > 152 * 32) grid = 152 * 32;
-  fixed_to_float_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(n3, force_fix, force);
+  fixed_to_float_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(n3, pdrag_fix, pdrag);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;

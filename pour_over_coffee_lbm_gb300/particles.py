@@ -84,7 +84,7 @@ class CoffeeParticleSystem:
         self._fix = None
         self.count = 0
         self._since_sort = None
-        self._reaction = None
+        self._solver = None
 
     # ---- seeding ---------------------------------------------------------------------------
     def seed(self, lattice: Optional[LatticeConfig] = None, config: Optional[ParticleConfig] = None):
@@ -126,9 +126,10 @@ class CoffeeParticleSystem:
         return self._keys[:n], (self._perm[:n] if sort else None)
 
     def couple(self, solver, dt: float = 1.0, relaxation_factor: float = 0.8,
-               force: Optional[torch.Tensor] = None):
+               pdrag: Optional[torch.Tensor] = None):
         """One coupling pass against solver's current velocity field: drag, under-relaxation,
-        reaction spread into `force` ([3, NZ, NY, NX], not cleared here), integration."""
+        integration, and the drag deposit (Kp, Kv) added into `pdrag` ([4, NZ, NY, NX], not
+        cleared here) for the implicit fluid-side force of the next lattice step."""
         n = self.count
         if n == 0:
             return
@@ -138,11 +139,11 @@ class CoffeeParticleSystem:
         pp = pc.to_c()
         pp.dt = float(dt)
         pp.relaxation = float(relaxation_factor)
-        f_out = force if force is not None else solver._force
+        f_out = pdrag if pdrag is not None else solver._pdrag
         fix = None
         if pc.deterministic:
-            if self._fix is None or self._fix.numel() != 3 * solver.n:
-                self._fix = torch.zeros(3 * solver.n, dtype=torch.int64, device=self.device)
+            if self._fix is None or self._fix.numel() != 4 * solver.n:
+                self._fix = torch.zeros(4 * solver.n, dtype=torch.int64, device=self.device)
             else:
                 self._fix.zero_()
             fix = self._fix
@@ -154,9 +155,9 @@ class CoffeeParticleSystem:
             _lib.ptr(self._u_at), s))
         if pc.deterministic:
             tmp = torch.empty_like(f_out)
-            _lib.check(self.lib.pog_force_from_fixed(solver._p, _lib.ptr(fix), _lib.ptr(tmp), s))
+            _lib.check(self.lib.pog_drag_from_fixed(solver._p, _lib.ptr(fix), _lib.ptr(tmp), s))
             f_out.add_(tmp)
-        self._reaction = f_out
+        self._solver = solver
         self._since_sort = (self._since_sort or 0) + 1
 
     # ---- reference accessors -----------------------------------------------------------------
@@ -202,10 +203,11 @@ class CoffeeParticleSystem:
 
     @property
     def reaction_force_field(self):
+        """Force density on the fluid from the last coupling (coffee_particles.py:45)."""
         from .solver import FieldView
-        if self._reaction is None:
+        if self._solver is None:
             raise AttributeError("no coupling step has run yet")
-        return FieldView(self._reaction, ncomp=3)
+        return FieldView(self._solver.particle_reaction_force(), ncomp=3, readonly=True)
 
     @property
     def particle_count(self):
@@ -240,8 +242,9 @@ class CoffeeParticleSystem:
         re = self._reynolds()[act]
         cd = (24.0 / re.clamp_min(0.01))
         mr = 0.0
-        if self._reaction is not None:
-            mr = float(torch.sqrt((self._reaction.double() ** 2).sum(0)).max())
+        if self._solver is not None:
+            rf = self._solver.particle_reaction_force()
+            mr = float(torch.sqrt((rf.double() ** 2).sum(0)).max())
         return {"active_particles": int(act.sum()),
                 "avg_reynolds": float(re.mean()) if re.numel() else 0.0,
                 "max_reynolds": float(re.max()) if re.numel() else 0.0,

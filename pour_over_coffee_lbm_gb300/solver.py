@@ -142,7 +142,8 @@ class GB300LBMSolver:
         _lib.check(self.lib.pog_validate_params(self._p))
         shape = (c.nz, c.ny, c.nx)
         dev = self.device
-        self._flags = torch.empty(shape, dtype=torch.uint8, device=dev)
+        # one 32-bit word per cell: flag bits + bit (8+q) when neighbour q is solid
+        self._flags = torch.empty(shape, dtype=torch.int32, device=dev)
         self._build_flags()
         self._f = torch.empty((19,) + shape, dtype=_STORAGE_DTYPE[c.storage], device=dev)
         self._rho = torch.ones(shape, dtype=torch.float32, device=dev)
@@ -154,6 +155,9 @@ class GB300LBMSolver:
             self._ul = [torch.zeros((3,) + shape, dtype=torch.float32, device=dev) for _ in range(2)]
         self._force = torch.zeros((3,) + shape, dtype=torch.float32, device=dev)
         self._force_active = False
+        # particle drag deposit (Kp, Kv_x, Kv_y, Kv_z) written by the coupling pass
+        self._pdrag = torch.zeros((4,) + shape, dtype=torch.float32, device=dev)
+        self._pdrag_active = False
         self._phase = torch.ones(shape, dtype=torch.float32, device=dev)
         self._red = torch.zeros(RED_COUNT, dtype=torch.float64, device=dev)
         self._porosity = None
@@ -183,6 +187,7 @@ class GB300LBMSolver:
             return
         _lib.check(self.lib.pog_macroscopic(self._p, _lib.ptr(self._f), _lib.ptr(self._flags),
                                             self.t, _lib.ptr(self._force) if self._force_active else None,
+                                            _lib.ptr(self._pdrag) if self._pdrag_active else None,
                                             _lib.ptr(self._rho), _lib.ptr(self._u), self._s()))
         self._macro_dirty = False
 
@@ -299,13 +304,14 @@ class GB300LBMSolver:
         if np.any(shell & ~mask):
             raise ValueError("the outer one-cell shell of the grid must be solid")
         solid = np.ascontiguousarray(mask.transpose(2, 1, 0))  # -> [z, y, x]
-        old = self._flags.cpu().numpy()
-        fl = np.where(solid, CELL_SOLID, old & (CELL_INLET | CELL_OUTLET | CELL_POROUS)).astype(np.uint8)
-        near = np.zeros_like(solid)
+        old = self._flags.cpu().numpy().astype(np.uint32)
+        fl = np.where(solid, CELL_SOLID, old & (CELL_INLET | CELL_OUTLET | CELL_POROUS)).astype(np.uint32)
+        links = np.zeros(solid.shape, np.uint32)
         for q in range(1, 19):
-            near |= np.roll(solid, shift=(-CZ[q], -CY[q], -CX[q]), axis=(0, 1, 2))
-        fl = np.where(~solid & near, fl | CELL_NEAR_SOLID, fl).astype(np.uint8)
-        self._flags.copy_(torch.from_numpy(fl))
+            nb_solid = np.roll(solid, shift=(-CZ[q], -CY[q], -CX[q]), axis=(0, 1, 2))
+            links |= nb_solid.astype(np.uint32) << np.uint32(8 + q)
+        fl = np.where(~solid & (links != 0), fl | CELL_NEAR_SOLID | links, fl).astype(np.uint32)
+        self._flags.copy_(torch.from_numpy(fl.astype(np.int32)))
         self.initialize_fields(self.cfg.rho0)
 
     def set_porosity(self, eps) -> None:
@@ -332,6 +338,7 @@ class GB300LBMSolver:
         _lib.check(self.lib.pog_step(
             self._p, _lib.ptr(self._f), _lib.ptr(self._flags), self.t, int(nsteps),
             _lib.ptr(self._force) if self._force_active else None,
+            _lib.ptr(self._pdrag) if self._pdrag_active else None,
             _lib.ptr(self._porosity), up, un,
             _lib.ptr(self._rho) if want_macro else None,
             _lib.ptr(self._u) if want_macro else None,
@@ -395,10 +402,19 @@ class GB300LBMSolver:
         spread into body_force, one LBM step with that force, particle integration.  With
         reduce=True returns the step's FP64 sums (mass, momentum, outflow, non-finite)."""
         self._refresh_macro()  # the coupling reads u of the current state
-        self._force.zero_()
-        particle_system.couple(self, dt=dt, relaxation_factor=relaxation_factor, force=self._force)
-        self._force_active = True
+        self.clear_body_force()  # legacy/lbm_solver.py:1489
+        self._pdrag.zero_()
+        particle_system.couple(self, dt=dt, relaxation_factor=relaxation_factor, pdrag=self._pdrag)
+        self._pdrag_active = True
         return self.run(1, want_macro=True, reduce=reduce)
+
+    def particle_reaction_force(self) -> torch.Tensor:
+        """Force density the particles exerted on the fluid in the last coupled step,
+        Kv - Kp u ([3, NZ, NY, NX]); zero before any coupled step."""
+        if not self._pdrag_active:
+            return torch.zeros_like(self._force)
+        self._refresh_macro()
+        return self._pdrag[1:] - self._pdrag[0:1] * self._u
 
     def set_inlet_control(self, control: Optional[torch.Tensor]) -> None:
         """Feed the pour from a device tensor [u_inlet, a_0..a_15] (float32, 17 values) that the
@@ -421,7 +437,8 @@ class GB300LBMSolver:
         self.step_with_two_way_coupling(particle_system)
 
     def compute_drag_force(self) -> FieldView:
-        return self.body_force
+        """ParticleCoupledLBMProtocol: the particles' force on the fluid (lbm_protocol.py:235)."""
+        return FieldView(self.particle_reaction_force(), ncomp=3, readonly=True)
 
     # ---- diagnostics ------------------------------------------------------------------------
     def conservation(self) -> dict:

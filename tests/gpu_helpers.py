@@ -34,7 +34,7 @@ def rel_l2(a, b):
 
 def gpu_flags(cfg):
     p = cfg.to_c()
-    fl = torch.empty((cfg.nz, cfg.ny, cfg.nx), dtype=torch.uint8, device="cuda")
+    fl = torch.empty((cfg.nz, cfg.ny, cfg.nx), dtype=torch.int32, device="cuda")
     _lib.check(lib().pog_build_flags(ctypes.byref(p), P(fl), S()))
     return fl
 
@@ -42,17 +42,18 @@ def gpu_flags(cfg):
 class AARun:
     """AA-pattern state driven through pog_step."""
 
-    def __init__(self, cfg, flags=None, eps=None, force=None):
+    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None):
         self.cfg = cfg
         self.p = cfg.to_c()
         shape = (cfg.nz, cfg.ny, cfg.nx)
-        self.flags = gpu_flags(cfg) if flags is None else torch.as_tensor(flags).cuda()
+        self.flags = gpu_flags(cfg) if flags is None else torch.as_tensor(np.asarray(flags).astype(np.int32)).cuda()
         self.f = torch.empty((19,) + shape, dtype=DT[cfg.storage], device="cuda")
         self.rho = torch.zeros(shape, dtype=torch.float32, device="cuda")
         self.u = torch.zeros((3,) + shape, dtype=torch.float32, device="cuda")
         self.ul = [torch.zeros((3,) + shape, dtype=torch.float32, device="cuda") for _ in range(2)]
         self.eps = None if eps is None else torch.as_tensor(np.asarray(eps, np.float32)).cuda()
         self.force = None if force is None else torch.as_tensor(np.asarray(force, np.float32)).cuda()
+        self.pdrag = None if pdrag is None else torch.as_tensor(np.asarray(pdrag, np.float32)).cuda()
         self.red = torch.zeros(RED_COUNT, dtype=torch.float64, device="cuda")
         self.t = 0
         _lib.check(lib().pog_init_equilibrium(ctypes.byref(self.p), P(self.f), P(self.flags),
@@ -61,7 +62,7 @@ class AARun:
     def step(self, n, reduce=False, macro=True):
         stencil = self.cfg.les_mode == LES_STENCIL
         _lib.check(lib().pog_step(ctypes.byref(self.p), P(self.f), P(self.flags), self.t, n,
-                                  P(self.force), P(self.eps),
+                                  P(self.force), P(self.pdrag), P(self.eps),
                                   P(self.ul[0]) if stencil else None, P(self.ul[1]) if stencil else None,
                                   P(self.rho) if macro else None, P(self.u) if macro else None,
                                   P(self.red) if reduce else None, S()))
@@ -78,8 +79,8 @@ class AARun:
         return nat.cpu().numpy()
 
 
-def run_aa(cfg, steps, eps=None, force=None, reduce=True):
-    r = AARun(cfg, eps=eps, force=force)
+def run_aa(cfg, steps, eps=None, force=None, reduce=True, pdrag=None):
+    r = AARun(cfg, eps=eps, force=force, pdrag=pdrag)
     if steps > 1:
         r.step(steps - 1, reduce=reduce, macro=False)
     r.step(1, reduce=reduce, macro=True)
@@ -102,7 +103,7 @@ def run_push(cfg, steps, flags=None, eps=None, reduce=True):
     red = torch.zeros(RED_COUNT, dtype=torch.float64, device="cuda")
     e = None if eps is None else torch.as_tensor(np.asarray(eps, np.float32)).cuda()
     for i in range(steps):
-        _lib.check(lib().pog_step_push(ctypes.byref(p), P(a), P(b), P(fl), None, P(e),
+        _lib.check(lib().pog_step_push(ctypes.byref(p), P(a), P(b), P(fl), None, None, P(e),
                                        P(up) if cfg.les_mode == LES_STENCIL else None,
                                        P(rho), P(u), P(red) if reduce else None, S()))
         up.copy_(u)

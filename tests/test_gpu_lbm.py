@@ -180,7 +180,7 @@ def test_macroscopic_matches_next_step_moments(cuda):
     r = run_aa(cfg, 11)
     rho = torch.empty_like(r.rho)
     u = torch.empty_like(r.u)
-    _lib.check(lib().pog_macroscopic(ctypes.byref(r.p), P(r.f), P(r.flags), r.t, None, P(rho), P(u), S()))
+    _lib.check(lib().pog_macroscopic(ctypes.byref(r.p), P(r.f), P(r.flags), r.t, None, None, P(rho), P(u), S()))
     r.step(1, macro=True)
     torch.cuda.synchronize()
     fluid = (r.flags & CELL_SOLID) == 0
@@ -192,13 +192,13 @@ def test_errors_are_reported(cuda):
     cfg = LatticeConfig(nx=16, ny=16, nz=16)
     p = cfg.to_c()
     fl = gpu_flags(cfg)
-    rc = lib().pog_step(ctypes.byref(p), None, P(fl), 0, 1, None, None, None, None, None, None, None, S())
+    rc = lib().pog_step(ctypes.byref(p), None, P(fl), 0, 1, None, None, None, None, None, None, None, None, S())
     assert rc == -1
     f = torch.empty((19, 16, 16, 16), device="cuda")
     p2 = cfg.replace(les_mode=LES_STENCIL).to_c()
-    rc = lib().pog_step(ctypes.byref(p2), P(f), P(fl), 0, 1, None, None, None, None, None, None, None, S())
+    rc = lib().pog_step(ctypes.byref(p2), P(f), P(fl), 0, 1, None, None, None, None, None, None, None, None, S())
     assert rc == -1 and b"u buffers" in lib().pog_last_error()
-    rc = lib().pog_step_push(ctypes.byref(p), P(f), P(f), P(fl), None, None, None, None, None, None, S())
+    rc = lib().pog_step_push(ctypes.byref(p), P(f), P(f), P(fl), None, None, None, None, None, None, None, S())
     assert rc == -1
 
 
@@ -211,12 +211,12 @@ sys.path.insert(0, %r)
 from pour_over_coffee_lbm_gb300 import _lib
 from pour_over_coffee_lbm_gb300.params import LatticeConfig
 cfg = LatticeConfig(nx=16, ny=16, nz=16); p = cfg.to_c(); L = _lib.load()
-fl = torch.empty((16,16,16), dtype=torch.uint8, device='cuda'); f = torch.empty((19,16,16,16), device='cuda')
+fl = torch.empty((16,16,16), dtype=torch.int32, device='cuda'); f = torch.empty((19,16,16,16), device='cuda')
 s = _lib.stream_handle()
 _lib.check(L.pog_build_flags(ctypes.byref(p), _lib.ptr(fl), s))
 _lib.check(L.pog_init_equilibrium(ctypes.byref(p), _lib.ptr(f), _lib.ptr(fl), 1.0, 0.0, 0.0, 0.0, s))
-assert L.pog_step(ctypes.byref(p), _lib.ptr(f), _lib.ptr(fl), 0, 3, None, None, None, None, None, None, None, s) == 0
-rc = L.pog_step(ctypes.byref(p), _lib.ptr(f), _lib.ptr(fl), 3, 3, None, None, None, None, None, None, None, s)
+assert L.pog_step(ctypes.byref(p), _lib.ptr(f), _lib.ptr(fl), 0, 3, None, None, None, None, None, None, None, None, s) == 0
+rc = L.pog_step(ctypes.byref(p), _lib.ptr(f), _lib.ptr(fl), 3, 3, None, None, None, None, None, None, None, None, s)
 assert rc == -4, rc
 torch.cuda.synchronize()
 print("ok")

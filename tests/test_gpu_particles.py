@@ -1,8 +1,8 @@
 """GPU parity of the particle path through the C ABI.
 
 Bit-exact: cell keys, the stable cell order (== numpy argsort(kind="stable")), and in
-deterministic mode every per-particle output plus the fixed-point force grid.  The float-atomic
-(warp-aggregated) force grid agrees with the fixed-point grid to FP32 summation error.
+deterministic mode every per-particle output plus the fixed-point drag deposit (Kp, Kv).  The
+float-atomic (warp-aggregated) deposit agrees with the fixed-point one to FP32 summation error.
 """
 import ctypes
 import os
@@ -39,8 +39,8 @@ def gpu_couple(cfg, pc, pos, vel, d, drag, act, u, order=None, deterministic=Tru
     T = lambda a, dt=np.float32: torch.as_tensor(np.ascontiguousarray(a, dt)).cuda()  # noqa: E731
     pos_t, vel_t, d_t, drag_t, act_t, u_t = T(pos), T(vel), T(d), T(drag), T(act, np.int32), T(u)
     ord_t = None if order is None else T(order, np.int32)
-    fix = torch.zeros(3 * cfg.ncell, dtype=torch.int64, device="cuda")
-    force = torch.zeros(3 * cfg.ncell, dtype=torch.float32, device="cuda")
+    fix = torch.zeros(4 * cfg.ncell, dtype=torch.int64, device="cuda")
+    force = torch.zeros(4 * cfg.ncell, dtype=torch.float32, device="cuda")
     uat = torch.zeros((3, n), dtype=torch.float32, device="cuda")
     _lib.check(lib().pog_particles_couple(ctypes.byref(p), ctypes.byref(pp), P(pos_t), P(vel_t), P(d_t),
                                           P(drag_t), P(act_t), n, P(ord_t), P(u_t),

@@ -99,8 +99,8 @@ def test_two_way_coupled_steps_vs_oracle(cuda, orc):
     _, _, u = orc.step(cfg, flags, f)
     for _ in range(steps):
         pos, vel, drag, act, fix, _ = orc.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
-        force = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(3, cfg.nz, cfg.ny, cfg.nx)
-        f, rho, u = orc.step(cfg, flags, f, force=force)
+        pdrag = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(4, cfg.nz, cfg.ny, cfg.nx)
+        f, rho, u = orc.step(cfg, flags, f, pdrag=pdrag)
     gpos = ps._pos[:, : pc.count].cpu().numpy()
     assert np.abs(gpos - pos).max() < 1e-4
     gu = s._u.cpu().numpy()
