@@ -46,6 +46,11 @@ KParams make_kparams(const pog_params* p) {
   k.guard_hi = k.n - 1 - k.guard_lo;
   for (int q = 0; q < 19; ++q)
     k.off[q] = cx(q) + cy(q) * (int32_t)k.nx + cz(q) * (int32_t)k.nxny;
+  for (int q = 0; q < 19; ++q) {
+    k.pl[q] = (uint32_t)q * k.n;
+    k.rd[q] = (uint32_t)opp(q) * k.n - (uint32_t)k.off[q];
+    k.wr[q] = (uint32_t)q * k.n + (uint32_t)k.off[q];
+  }
   k.les_mode = p->les_mode;
   k.drag_mode = p->drag_mode;
   k.forcing_mode = p->forcing_mode;

@@ -315,15 +315,20 @@ struct Store<POG_STORE_F64> {
   __device__ static __forceinline__ C ld(const E* p, uint32_t i, int, C) { return p[i]; }
   __device__ static __forceinline__ void st(E* p, uint32_t i, int, C v, C) { p[i] = v; }
 };
+// 16-bit storages hold the shifted form f - w_q rho0 (FP16 scaled by 2^12).  The decode is one
+// rounding of w + h 2^-12 and the encode rounds (f - w) 2^12 once before the 16-bit rounding,
+// w = fl(w_q rho0): the same roundings, in the same order, as the oracle's storage emulation.
 template <>
 struct Store<POG_STORE_F16S> {
   using E = __half;
   using C = float;
   __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C rho0) {
-    return (float)wd(q) * rho0 + __half2float(p[i]) * F16_INV_SCALE;
+    const float w = __fmul_rn((float)wd(q), rho0);
+    return __fmaf_rn(__half2float(p[i]), F16_INV_SCALE, w);
   }
   __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C rho0) {
-    p[i] = __float2half_rn((v - (float)wd(q) * rho0) * F16_SCALE);
+    const float w = __fmul_rn((float)wd(q), rho0);
+    p[i] = __float2half_rn(__fmaf_rn(v, F16_SCALE, -w * F16_SCALE));
   }
 };
 template <>
@@ -331,12 +336,79 @@ struct Store<POG_STORE_BF16S> {
   using E = __nv_bfloat16;
   using C = float;
   __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C rho0) {
-    return (float)wd(q) * rho0 + __bfloat162float(p[i]);
+    return __fadd_rn(__bfloat162float(p[i]), __fmul_rn((float)wd(q), rho0));
   }
   __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C rho0) {
-    p[i] = __float2bfloat16_rn(v - (float)wd(q) * rho0);
+    p[i] = __float2bfloat16_rn(__fsub_rn(v, __fmul_rn((float)wd(q), rho0)));
   }
 };
+
+// Per-thread partial sums of the POG_RED_* slots (mass, momentum, outflow, non-finite count).
+// GB300 issues FP64 arithmetic at a small fraction of the FP32 rate, so FP32 cells accumulate in
+// double-float form: an unevaluated sum hi + lo of two floats, updated with error-free
+// transformations (Knuth's TwoSum; the product rho*u split exactly by one FMA).  The partial
+// carries ~48 significant bits; FP64 is used once per thread, when the partials enter the block
+// reduction.  FP64 cells accumulate in FP64.
+template <typename C>
+struct RedAcc {
+  double s[POG_RED_COUNT];
+  __device__ __forceinline__ RedAcc() {
+#pragma unroll
+    for (int r = 0; r < POG_RED_COUNT; ++r) s[r] = 0.0;
+  }
+  __device__ __forceinline__ void add(const CellResult<C>& r) {
+    s[POG_RED_MASS] += (double)r.rho;
+    s[POG_RED_MOMX] += (double)r.rho * (double)r.ux;
+    s[POG_RED_MOMY] += (double)r.rho * (double)r.uy;
+    s[POG_RED_MOMZ] += (double)r.rho * (double)r.uz;
+    s[POG_RED_OUTFLOW] += (double)r.outflow;
+    const bool bad = !(isfinite((double)r.rho) && isfinite((double)r.ux) && isfinite((double)r.uy) &&
+                       isfinite((double)r.uz));
+    s[POG_RED_NONFINITE] += bad ? 1.0 : 0.0;
+  }
+  __device__ __forceinline__ void finish(double out[POG_RED_COUNT]) const {
+#pragma unroll
+    for (int r = 0; r < POG_RED_COUNT; ++r) out[r] = s[r];
+  }
+};
+
+template <>
+struct RedAcc<float> {
+  float hi[POG_RED_COUNT - 1], lo[POG_RED_COUNT - 1];
+  unsigned bad;
+  __device__ __forceinline__ RedAcc() : bad(0u) {
+#pragma unroll
+    for (int r = 0; r < POG_RED_COUNT - 1; ++r) hi[r] = lo[r] = 0.0f;
+  }
+  // (hi, lo) += x without rounding loss: TwoSum gives s + e == hi + x exactly
+  __device__ static __forceinline__ void two_sum(float& h, float& l, float x) {
+    const float s = __fadd_rn(h, x);
+    const float bv = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bv)), __fsub_rn(x, bv));
+    h = s;
+    l = __fadd_rn(l, e);
+  }
+  __device__ static __forceinline__ void two_prod_sum(float& h, float& l, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);  // a*b == p + pe exactly
+    two_sum(h, l, p);
+    l = __fadd_rn(l, pe);
+  }
+  __device__ __forceinline__ void add(const CellResult<float>& r) {
+    two_sum(hi[POG_RED_MASS], lo[POG_RED_MASS], r.rho);
+    two_prod_sum(hi[POG_RED_MOMX], lo[POG_RED_MOMX], r.rho, r.ux);
+    two_prod_sum(hi[POG_RED_MOMY], lo[POG_RED_MOMY], r.rho, r.uy);
+    two_prod_sum(hi[POG_RED_MOMZ], lo[POG_RED_MOMZ], r.rho, r.uz);
+    two_sum(hi[POG_RED_OUTFLOW], lo[POG_RED_OUTFLOW], r.outflow);
+    bad += (isfinite(r.rho) && isfinite(r.ux) && isfinite(r.uy) && isfinite(r.uz)) ? 0u : 1u;
+  }
+  __device__ __forceinline__ void finish(double out[POG_RED_COUNT]) const {
+#pragma unroll
+    for (int r = 0; r < POG_RED_COUNT - 1; ++r) out[r] = (double)hi[r] + (double)lo[r];
+    out[POG_RED_NONFINITE] = (double)bad;
+  }
+};
+static_assert(POG_RED_NONFINITE == POG_RED_COUNT - 1, "the count slot is last");
 
 // FP64 block reduction of the POG_RED_* slots: warp shuffles, shared memory, one atomic per
 // block and slot.  All threads of the block must call it.

@@ -48,6 +48,11 @@ struct KParams {
   // malformed flags (a fluid cell on the outer shell) cannot drive an access out of bounds.
   uint32_t guard_lo, guard_hi;
   int32_t off[19];         // neighbour offset of direction q in cells
+  // Element offsets relative to a cell's own element c (all non-negative, < 19 n < 2^32):
+  //   pl[q] = q n              slot (c, q)
+  //   rd[q] = opp(q) n - off[q] odd-step streaming read (c - e_q, opp q)
+  //   wr[q] = q n + off[q]      odd-step streaming write (c + e_q, q)
+  uint32_t pl[19], rd[19], wr[19];
   int32_t les_mode, drag_mode, forcing_mode, clamp_tau, storage;
   float tau, rho0, gx, gy, gz;
   float cs2, strain_floor, nu_max, tau_min, tau_max, nu0;

@@ -15,8 +15,10 @@
 // the post-collision f*_q to (c, opp q): no neighbour access at all.  Odd step: read f_q from
 // (c - e_q, opp q) -- or from (c, q) when c - e_q is solid (half-way bounce-back) -- and write
 // f*_q to (c + e_q, q) -- or to (c, opp q) when c + e_q is solid.  A cell reads and writes the
-// same 19 slots, so the update is in place and race-free.  The NEAR_SOLID flag bit lets cells
-// away from walls skip the 18 neighbour-flag reads.
+// same 19 slots, so the update is in place and race-free.  Which neighbours are solid comes from
+// the 18 link bits of the cell's own flag word: a cell without any takes the odd step's plain
+// streaming addresses (per-direction offset tables, no per-direction tests), the others choose
+// per direction between the streamed and the bounced slot.
 #include "collide.cuh"
 
 namespace pog {
@@ -41,25 +43,26 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
   using C = typename St::C;
   const C rho0 = (C)kp.rho0;
   const uint32_t n = kp.n;
-  double acc[POG_RED_COUNT];
-  if (REDUCE) {
-#pragma unroll
-    for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] = 0.0;
-  }
+  RedAcc<C> acc;
   for (uint32_t c = blockIdx.x * AA_BLOCK + threadIdx.x; c < n; c += gridDim.x * AA_BLOCK) {
     const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
+    // every slot of cell c sits at fc + (a non-negative offset below 19 n) from the tables
+    typename St::E* const fc = f + c;
+    const bool open = (fl >> POG_LINK_SHIFT) == 0u;  // no solid neighbour
     C fv[19];
     if (PARITY == 0) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) fv[q] = St::ld(f, (uint32_t)q * n + c, q, rho0);
+    } else if (open) {
+#pragma unroll
+      for (int q = 0; q < 19; ++q) fv[q] = St::ld(fc, kp.rd[q], q, rho0);
     } else {
       // source c - e_q is the neighbour in direction opp(q); a solid one bounces f_q back
 #pragma unroll
       for (int q = 0; q < 19; ++q) {
         const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
-        const uint32_t idx = wall ? (uint32_t)q * n + c : (uint32_t)opp(q) * n + (c - (uint32_t)kp.off[q]);
-        fv[q] = St::ld(f, idx, q, rho0);
+        fv[q] = St::ld(fc, wall ? kp.pl[q] : kp.rd[q], q, rho0);
       }
     }
     C nu_st = (C)0;
@@ -78,29 +81,28 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
       u_next[2u * n + c] = (float)r.uz;
     }
     if (REDUCE) {
-      acc[POG_RED_MASS] += (double)r.rho;
-      acc[POG_RED_MOMX] += (double)r.rho * (double)r.ux;
-      acc[POG_RED_MOMY] += (double)r.rho * (double)r.uy;
-      acc[POG_RED_MOMZ] += (double)r.rho * (double)r.uz;
-      acc[POG_RED_OUTFLOW] += (double)r.outflow;
-      const bool bad = !(isfinite((double)r.rho) && isfinite((double)r.ux) &&
-                         isfinite((double)r.uy) && isfinite((double)r.uz));
-      acc[POG_RED_NONFINITE] += bad ? 1.0 : 0.0;
+      acc.add(r);
     }
     if (MACRO_ONLY) continue;
     if (PARITY == 0) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) St::st(f, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
+    } else if (open) {
+#pragma unroll
+      for (int q = 0; q < 19; ++q) St::st(fc, kp.wr[q], q, fv[q], rho0);
     } else {
 #pragma unroll
       for (int q = 0; q < 19; ++q) {
         const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
-        const uint32_t idx = wall ? (uint32_t)opp(q) * n + c : (uint32_t)q * n + (c + (uint32_t)kp.off[q]);
-        St::st(f, idx, q, fv[q], rho0);
+        St::st(fc, wall ? kp.pl[opp(q)] : kp.wr[q], q, fv[q], rho0);
       }
     }
   }
-  if (REDUCE) block_reduce_add(acc, red);
+  if (REDUCE) {
+    double part[POG_RED_COUNT];
+    acc.finish(part);
+    block_reduce_add(part, red);
+  }
 }
 
 // Natural-layout copy of the AA state at parity PARITY (odd = the odd-step read gather).

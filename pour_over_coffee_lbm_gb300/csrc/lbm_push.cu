@@ -19,11 +19,7 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
   using C = typename St::C;
   const C rho0 = (C)kp.rho0;
   const uint32_t n = kp.n;
-  double acc[POG_RED_COUNT];
-  if (REDUCE) {
-#pragma unroll
-    for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] = 0.0;
-  }
+  RedAcc<C> acc;
   for (uint32_t c = blockIdx.x * PUSH_BLOCK + threadIdx.x; c < n; c += gridDim.x * PUSH_BLOCK) {
     const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
@@ -41,14 +37,7 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
       u_out[2u * n + c] = (float)r.uz;
     }
     if (REDUCE) {
-      acc[POG_RED_MASS] += (double)r.rho;
-      acc[POG_RED_MOMX] += (double)r.rho * (double)r.ux;
-      acc[POG_RED_MOMY] += (double)r.rho * (double)r.uy;
-      acc[POG_RED_MOMZ] += (double)r.rho * (double)r.uz;
-      acc[POG_RED_OUTFLOW] += (double)r.outflow;
-      const bool bad = !(isfinite((double)r.rho) && isfinite((double)r.ux) &&
-                         isfinite((double)r.uy) && isfinite((double)r.uz));
-      acc[POG_RED_NONFINITE] += bad ? 1.0 : 0.0;
+      acc.add(r);
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
@@ -60,7 +49,11 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
         St::st(fout, (uint32_t)q * n + dst, q, fv[q], rho0);
     }
   }
-  if (REDUCE) block_reduce_add(acc, red);
+  if (REDUCE) {
+    double part[POG_RED_COUNT];
+    acc.finish(part);
+    block_reduce_add(part, red);
+  }
 }
 
 template <int S, bool R>

@@ -134,9 +134,7 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
   __syncthreads();
   const uint32_t first = blockIdx.x, stride = gridDim.x;
   const uint32_t nit = first < ntiles ? (ntiles - first + stride - 1) / stride : 0;
-  double acc[POG_RED_COUNT];
-#pragma unroll
-  for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] = 0.0;
+  RedAcc<C> acc;
 
   if (warp == NCW) {
     // ---------------- producer ----------------
@@ -202,14 +200,7 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
         u_next[2u * n + c] = (float)r.uz;
       }
       if (REDUCE) {
-        acc[POG_RED_MASS] += (double)r.rho;
-        acc[POG_RED_MOMX] += (double)r.rho * (double)r.ux;
-        acc[POG_RED_MOMY] += (double)r.rho * (double)r.uy;
-        acc[POG_RED_MOMZ] += (double)r.rho * (double)r.uz;
-        acc[POG_RED_OUTFLOW] += (double)r.outflow;
-        const bool bad = !(isfinite((double)r.rho) && isfinite((double)r.ux) &&
-                           isfinite((double)r.uy) && isfinite((double)r.uz));
-        acc[POG_RED_NONFINITE] += bad ? 1.0 : 0.0;
+        acc.add(r);
       }
       if (PARITY == 0) {
 #pragma unroll
@@ -226,7 +217,11 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
   }
   if (REDUCE) {
     __syncthreads();
-    if (!s_abort) block_reduce_add(acc, red);
+    if (!s_abort) {
+      double part[POG_RED_COUNT];
+      acc.finish(part);
+      block_reduce_add(part, red);
+    }
   }
 }
 
