@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--error-steps", type=int, default=2000, help="steps of the FP64 error runs")
     ap.add_argument("--small", action="store_true", help="64^3 / 2,000 particles (profiling)")
+    ap.add_argument("--precision-only", choices=["fp32", "fp16s", "bf16s"], default=None,
+                    help="time only the 256^3 precision case in this storage for --steps steps (profiling)")
     return ap.parse_args()
 
 
@@ -477,9 +479,20 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision_only(args):
+    import torch
+    from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
+    torch.cuda.set_device(0)
+    st = {"fp32": STORE_F32, "fp16s": STORE_F16S, "bf16s": STORE_BF16S}[args.precision_only]
+    out = precision_line(st, max(GRAPH_STEPS, args.steps), peaks())
+    print(json.dumps({"precision_only": args.precision_only, **out}), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.precision_only:
+        run_precision_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

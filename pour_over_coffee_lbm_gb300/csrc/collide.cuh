@@ -58,42 +58,66 @@ __host__ __device__ __forceinline__ C feq_q(int q, C rho, C ux, C uy, C uz, C us
   return (C)wd(q) * rho * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - usq15);
 }
 
-// One direction pair (q, opp q) of the BGK + Guo collision, q with e = (ex, ey, ez).
-//   keep = 1 - omega, a1 = omega w rho, b3 = 3 A w (A = 1 - omega/2), b3uF = b3 uF, base = 1 - 1.5 u.u
+// One direction pair (q, opp q) of the BGK + Guo collision, q with e = (ex, ey, ez), written as
+// a chain of FMAs.  Per weight class w (a1 = omega w rho, b3 = 3 (1 - omega/2) w):
+//   omega f_eq + S, even in e:  sym  = A + (e.u)(B e.u + Cc e.F),  A = a1 (1 - 1.5 u.u) - b3 u.F,
+//                                                                  B = 4.5 a1, Cc = 3 b3
+//   omega f_eq + S, odd in e:   asym = D e.u + b3 e.F,             D = 3 a1
+//   f*_q = (1 - omega) f_q + sym + asym,  f*_opp = (1 - omega) f_opp + sym - asym.
+template <typename C>
+struct PairCoef {
+  C A, B, Cc, D, b3;
+};
+template <typename C>
+__host__ __device__ __forceinline__ PairCoef<C> pair_coef(C a1, C b3, C uF, C base) {
+  PairCoef<C> k;
+  k.A = a1 * base - b3 * uF;
+  k.B = (C)4.5 * a1;
+  k.Cc = (C)3 * b3;
+  k.D = (C)3 * a1;
+  k.b3 = b3;
+  return k;
+}
 template <int Q, typename C>
-__host__ __device__ __forceinline__ void collide_pair(C f[19], C ux, C uy, C uz, C Fx, C Fy, C Fz,
-                                                      C keep, C a1, C b3, C b3uF, C base) {
+__host__ __device__ __forceinline__ void collide_pair(C f[19], C ux, C uy, C uz, C Fx, C Fy, C Fz, C keep,
+                                                      const PairCoef<C>& k) {
   constexpr int P = opp(Q);
   const C eu = (C)cx(Q) * ux + (C)cy(Q) * uy + (C)cz(Q) * uz;
   const C eF = (C)cx(Q) * Fx + (C)cy(Q) * Fy + (C)cz(Q) * Fz;
-  // even part: omega feq_s + S_s = a1 (base + 4.5 eu^2) + b3 (3 eu eF - uF)
-  const C sym = a1 * (base + (C)4.5 * eu * eu) + b3 * ((C)3 * eu * eF) - b3uF;
-  // odd part: omega feq_a + S_a = 3 a1 eu + b3 eF
-  const C asym = (C)3 * a1 * eu + b3 * eF;
+  const C sym = fma(eu, fma(k.Cc, eF, k.B * eu), k.A);
+  const C asym = fma(k.D, eu, k.b3 * eF);
   const C fq = f[Q], fp = f[P];
-  f[Q] = keep * fq + (sym + asym);
-  f[P] = keep * fp + (sym - asym);
+  f[Q] = fma(keep, fq, sym + asym);
+  f[P] = fma(keep, fp, sym - asym);
 }
 
 // f[19]: incoming populations on entry, post-collision populations on exit.
+// SH (shifted): f holds h_q = (f_q - w_q rho0) / sc instead of f_q, in and out -- the form the
+// 16-bit storages keep.  Moments, Pi_neq and the post-collision update are rewritten for h (the
+// shift and scale fold into per-cell coefficients), so no population is ever converted back.
 // nu_st: nu_sgs from the velocity stencil (LES_STENCIL mode), computed by the caller.
 // pdrag: [4][n] particle drag deposit (Kp = sum w beta, Kv = sum w beta v_p) or null; the
 // particle force on the fluid, Kv - Kp u, is taken implicitly in u (stable at any loading).
-template <typename C>
+template <typename C, bool SH = false>
 __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp, uint32_t fl, uint32_t c,
                                                                C f[19], const float* __restrict__ force,
                                                                const float* __restrict__ pdrag,
-                                                               const float* __restrict__ eps, C nu_st) {
+                                                               const float* __restrict__ eps, C nu_st,
+                                                               C sc = (C)1) {
   CellResult<C> res;
-  // ---- moments from one sweep of adds -------------------------------------------------------
+  const C rho0 = (C)kp.rho0;
+  // ---- moments from one sweep of adds (of h when SH: sum w = 1, sum w e = 0, sum w e e = I/3) --
   const C sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
   const C sxy = (f[7] + f[8]) + (f[9] + f[10]);
   const C sxz = (f[11] + f[12]) + (f[13] + f[14]);
   const C syz = (f[15] + f[16]) + (f[17] + f[18]);
-  const C rho = f[0] + (sx + sy) + (sz + sxy) + (sxz + syz);
-  const C mx = (f[1] - f[2]) + ((f[7] - f[8]) + (f[9] - f[10])) + ((f[11] - f[12]) + (f[13] - f[14]));
-  const C my = (f[3] - f[4]) + ((f[7] + f[8]) - (f[9] + f[10])) + ((f[15] - f[16]) + (f[17] - f[18]));
-  const C mz = (f[5] - f[6]) + ((f[11] + f[12]) - (f[13] + f[14])) + ((f[15] + f[16]) - (f[17] + f[18]));
+  const C rsum = f[0] + (sx + sy) + (sz + sxy) + (sxz + syz);
+  const C mxs = (f[1] - f[2]) + ((f[7] - f[8]) + (f[9] - f[10])) + ((f[11] - f[12]) + (f[13] - f[14]));
+  const C mys = (f[3] - f[4]) + ((f[7] + f[8]) - (f[9] + f[10])) + ((f[15] - f[16]) + (f[17] - f[18]));
+  const C mzs = (f[5] - f[6]) + ((f[11] + f[12]) - (f[13] + f[14])) + ((f[15] + f[16]) - (f[17] + f[18]));
+  const C rho = SH ? fma(sc, rsum, rho0) : rsum;
+  const C mx = SH ? sc * mxs : mxs, my = SH ? sc * mys : mys, mz = SH ? sc * mzs : mzs;
+  const C inv_sc = SH ? (C)1 / sc : (C)1;
   res.outflow = (C)0;
   if (fl & (POG_CELL_INLET | POG_CELL_OUTLET)) {
     C ux, uy, uz, rr;
@@ -111,7 +135,10 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     }
     C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[q] = feq_q<C>(q, rr, ux, uy, uz, usq15);
+    for (int q = 0; q < 19; ++q) {
+      const C fe = feq_q<C>(q, rr, ux, uy, uz, usq15);
+      f[q] = SH ? (fe - (C)wd(q) * rho0) * inv_sc : fe;
+    }
     res.rho = rho;
     res.ux = ux;
     res.uy = uy;
@@ -202,13 +229,15 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   C nu = (C)0;
   if (kp.les_mode == POG_LES_LOCAL && !porous) {
     // Pi_neq = sum e e f - rho (u u + I/3)
-    const C r3 = rho * (C)(1.0 / 3.0);
-    const C Pxx = (sx + sxy + sxz) - (rho * ux * ux + r3);
-    const C Pyy = (sy + sxy + syz) - (rho * uy * uy + r3);
-    const C Pzz = (sz + sxz + syz) - (rho * uz * uz + r3);
-    const C Pxy = ((f[7] - f[8]) - (f[9] - f[10])) - rho * ux * uy;
-    const C Pxz = ((f[11] - f[12]) - (f[13] - f[14])) - rho * ux * uz;
-    const C Pyz = ((f[15] - f[16]) - (f[17] - f[18])) - rho * uy * uz;
+    // SH: sum e_a e_b f = rho0/3 delta_ab + sc sum e_a e_b h
+    const C r3 = (SH ? rho - rho0 : rho) * (C)(1.0 / 3.0);
+    const C m2 = SH ? sc : (C)1;
+    const C Pxx = m2 * (sx + sxy + sxz) - (rho * ux * ux + r3);
+    const C Pyy = m2 * (sy + sxy + syz) - (rho * uy * uy + r3);
+    const C Pzz = m2 * (sz + sxz + syz) - (rho * uz * uz + r3);
+    const C Pxy = m2 * ((f[7] - f[8]) - (f[9] - f[10])) - rho * ux * uy;
+    const C Pxz = m2 * ((f[11] - f[12]) - (f[13] - f[14])) - rho * ux * uz;
+    const C Pyz = m2 * ((f[15] - f[16]) - (f[17] - f[18])) - rho * uy * uz;
     const C PP = Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + (C)2 * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz);
     const C Q = sqrt((C)2 * PP);
     const C tl = (C)0.5 * (tau0 + sqrt(tau0 * tau0 + (C)18 * (C)kp.cs2 * Q * inv_rho));
@@ -233,17 +262,28 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     const C a1_0 = or_ * (C)(1.0 / 3.0), a1_1 = or_ * (C)(1.0 / 18.0), a1_2 = or_ * (C)(1.0 / 36.0);
     const C b3_0 = A, b3_1 = A * (C)(3.0 / 18.0), b3_2 = A * (C)(3.0 / 36.0);
     // rest population: f0* = keep f0 + omega w0 rho base - 3 A w0 uF
-    f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF);
-    const C b3uF_1 = b3_1 * uF, b3uF_2 = b3_2 * uF;
-    collide_pair<1, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_1, b3_1, b3uF_1, base);
-    collide_pair<3, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_1, b3_1, b3uF_1, base);
-    collide_pair<5, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_1, b3_1, b3uF_1, base);
-    collide_pair<7, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
-    collide_pair<8, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
-    collide_pair<11, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
-    collide_pair<12, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
-    collide_pair<15, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
-    collide_pair<16, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, a1_2, b3_2, b3uF_2, base);
+    PairCoef<C> k1 = pair_coef<C>(a1_1, b3_1, uF, base), k2 = pair_coef<C>(a1_2, b3_2, uF, base);
+    if (SH) {
+      // h* = keep h + (omega f_eq + S - omega w rho0) / sc: subtract omega w rho0 from the even
+      // part and scale every coefficient by 1/sc
+      const C or0 = omega * rho0;
+      f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF - or0 * (C)(1.0 / 3.0)) * inv_sc;
+      k1.A = (k1.A - or0 * (C)(1.0 / 18.0)) * inv_sc;
+      k2.A = (k2.A - or0 * (C)(1.0 / 36.0)) * inv_sc;
+      k1.B *= inv_sc; k1.Cc *= inv_sc; k1.D *= inv_sc; k1.b3 *= inv_sc;
+      k2.B *= inv_sc; k2.Cc *= inv_sc; k2.D *= inv_sc; k2.b3 *= inv_sc;
+    } else {
+      f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF);
+    }
+    collide_pair<1, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+    collide_pair<3, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+    collide_pair<5, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+    collide_pair<7, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+    collide_pair<8, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+    collide_pair<11, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+    collide_pair<12, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+    collide_pair<15, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+    collide_pair<16, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
   } else {
     const C usq15 = (C)1.5 * usq;
     C taus = tau < (C)0.6 ? (C)0.6 : (tau > (C)1.5 ? (C)1.5 : tau);
@@ -265,7 +305,12 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
         S = S < (C)-0.5 ? (C)-0.5 : (S > (C)0.5 ? (C)0.5 : S);
       }
       const C fe = feq_q<C>(q, rho, ux, uy, uz, usq15);
-      f[q] = fe + keep * (f[q] - fe) + S;
+      if (SH) {
+        const C he = (fe - (C)wd(q) * rho0) * inv_sc;
+        f[q] = he + keep * (f[q] - he) + S * inv_sc;
+      } else {
+        f[q] = fe + keep * (f[q] - fe) + S;
+      }
     }
   }
   res.rho = rho;
@@ -301,46 +346,73 @@ __host__ __device__ __forceinline__ C les_nu_stencil(const KParams& kp, uint32_t
 // ---- storage formats ------------------------------------------------------------------------
 template <int S>
 struct Store;
+// dec/enc convert between a stored value and f_q; dech/ench between a stored value and the form
+// collide_cell<C, SHIFTED> works on (f_q itself, or h_q = (f_q - w_q rho0) / SCALE when SHIFTED).
 template <>
 struct Store<POG_STORE_F32> {
   using E = float;
   using C = float;
-  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int, C) { return p[i]; }
-  __device__ static __forceinline__ void st(E* p, uint32_t i, int, C v, C) { p[i] = v; }
+  static constexpr bool SHIFTED = false;
+  static constexpr float SCALE = 1.0f;
+  __device__ static __forceinline__ C dec(E v, int, C) { return v; }
+  __device__ static __forceinline__ E enc(C v, int, C) { return v; }
+  __device__ static __forceinline__ C dech(E v) { return v; }
+  __device__ static __forceinline__ E ench(C v) { return v; }
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C r) { return dec(p[i], q, r); }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C r) { p[i] = enc(v, q, r); }
 };
 template <>
 struct Store<POG_STORE_F64> {
   using E = double;
   using C = double;
-  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int, C) { return p[i]; }
-  __device__ static __forceinline__ void st(E* p, uint32_t i, int, C v, C) { p[i] = v; }
+  static constexpr bool SHIFTED = false;
+  static constexpr float SCALE = 1.0f;
+  __device__ static __forceinline__ C dec(E v, int, C) { return v; }
+  __device__ static __forceinline__ E enc(C v, int, C) { return v; }
+  __device__ static __forceinline__ C dech(E v) { return v; }
+  __device__ static __forceinline__ E ench(C v) { return v; }
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C r) { return dec(p[i], q, r); }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C r) { p[i] = enc(v, q, r); }
 };
-// 16-bit storages hold the shifted form f - w_q rho0 (FP16 scaled by 2^12).  The decode is one
-// rounding of w + h 2^-12 and the encode rounds (f - w) 2^12 once before the 16-bit rounding,
-// w = fl(w_q rho0): the same roundings, in the same order, as the oracle's storage emulation.
+// 16-bit storages hold the shifted form h = (f - w_q rho0) / SCALE (FP16: SCALE = 2^-12 keeps
+// small deviations normal; BF16: SCALE = 1).  dec is one rounding of w + h SCALE and enc rounds
+// (f - w) / SCALE once before the 16-bit rounding, w = fl(w_q rho0): the same roundings, in the
+// same order, as the oracle's storage emulation.  The step kernel skips dec/enc altogether and
+// collides h directly (dech/ench are the bare 16-bit conversions).
 template <>
 struct Store<POG_STORE_F16S> {
   using E = __half;
   using C = float;
-  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C rho0) {
-    const float w = __fmul_rn((float)wd(q), rho0);
-    return __fmaf_rn(__half2float(p[i]), F16_INV_SCALE, w);
+  static constexpr bool SHIFTED = true;
+  static constexpr float SCALE = F16_INV_SCALE;
+  __device__ static __forceinline__ C dec(E v, int q, C rho0) {
+    return __fmaf_rn(__half2float(v), F16_INV_SCALE, __fmul_rn((float)wd(q), rho0));
   }
-  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C rho0) {
+  __device__ static __forceinline__ E enc(C v, int q, C rho0) {
     const float w = __fmul_rn((float)wd(q), rho0);
-    p[i] = __float2half_rn(__fmaf_rn(v, F16_SCALE, -w * F16_SCALE));
+    return __float2half_rn(__fmaf_rn(v, F16_SCALE, -w * F16_SCALE));
   }
+  __device__ static __forceinline__ C dech(E v) { return __half2float(v); }
+  __device__ static __forceinline__ E ench(C v) { return __float2half_rn(v); }
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C r) { return dec(p[i], q, r); }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C r) { p[i] = enc(v, q, r); }
 };
 template <>
 struct Store<POG_STORE_BF16S> {
   using E = __nv_bfloat16;
   using C = float;
-  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C rho0) {
-    return __fadd_rn(__bfloat162float(p[i]), __fmul_rn((float)wd(q), rho0));
+  static constexpr bool SHIFTED = true;
+  static constexpr float SCALE = 1.0f;
+  __device__ static __forceinline__ C dec(E v, int q, C rho0) {
+    return __fadd_rn(__bfloat162float(v), __fmul_rn((float)wd(q), rho0));
   }
-  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C rho0) {
-    p[i] = __float2bfloat16_rn(__fsub_rn(v, __fmul_rn((float)wd(q), rho0)));
+  __device__ static __forceinline__ E enc(C v, int q, C rho0) {
+    return __float2bfloat16_rn(__fsub_rn(v, __fmul_rn((float)wd(q), rho0)));
   }
+  __device__ static __forceinline__ C dech(E v) { return __bfloat162float(v); }
+  __device__ static __forceinline__ E ench(C v) { return __float2bfloat16_rn(v); }
+  __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C r) { return dec(p[i], q, r); }
+  __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C r) { p[i] = enc(v, q, r); }
 };
 
 // Per-thread partial sums of the POG_RED_* slots (mass, momentum, outflow, non-finite count).

@@ -33,6 +33,79 @@ constexpr int AA_BLOCK = 256;
 #define POG_AA_ONE_CELL 1
 #endif
 
+// The 19 incoming populations of cell c as stored values (AA read pattern of PARITY).  Every
+// slot of cell c is element c + (a non-negative offset below 19 n) of the offset tables.  The odd
+// step takes the streaming offsets alone when no cell of the warp touches a solid neighbour (one
+// warp-uniform test); otherwise each direction chooses its streamed or bounced slot.
+template <int S, int PARITY>
+__device__ __forceinline__ void aa_load(const KParams& kp, const typename Store<S>::E* __restrict__ f,
+                                        uint32_t c, uint32_t fl, typename Store<S>::E raw[19]) {
+  if (PARITY == 0) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) raw[q] = f[(uint32_t)q * kp.n + c];
+  } else if (__all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u)) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) raw[q] = f[c + kp.rd[q]];
+  } else {
+    // source c - e_q is the neighbour in direction opp(q); a solid one bounces f_q back
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
+      raw[q] = f[c + (wall ? kp.pl[q] : kp.rd[q])];
+    }
+  }
+}
+
+// Collision of cell c (populations fv), its macroscopic outputs and sums, and the AA stores of
+// the post-collision populations (MACRO_ONLY: outputs only).
+template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
+__device__ __forceinline__ void aa_update(const KParams& kp, typename Store<S>::E* __restrict__ f,
+                                          uint32_t c, uint32_t fl, typename Store<S>::C fv[19],
+                                          const float* __restrict__ force, const float* __restrict__ pdrag,
+                                          const float* __restrict__ eps, const float* __restrict__ u_prev,
+                                          float* __restrict__ u_next, float* __restrict__ rho_out,
+                                          float* __restrict__ u_out, RedAcc<typename Store<S>::C>& acc) {
+  using St = Store<S>;
+  using C = typename St::C;
+  const C rho0 = (C)kp.rho0;
+  const uint32_t n = kp.n;
+  C nu_st = (C)0;
+  if (!MACRO_ONLY && kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS))
+    nu_st = les_nu_stencil<C>(kp, c, u_prev);
+  const CellResult<C> r = collide_cell<C, St::SHIFTED>(kp, fl, c, fv, force, pdrag, eps, nu_st, (C)St::SCALE);
+  if (rho_out) rho_out[c] = (float)r.rho;
+  if (u_out) {
+    u_out[c] = (float)r.ux;
+    u_out[n + c] = (float)r.uy;
+    u_out[2u * n + c] = (float)r.uz;
+  }
+  if (!MACRO_ONLY && u_next) {
+    u_next[c] = (float)r.ux;
+    u_next[n + c] = (float)r.uy;
+    u_next[2u * n + c] = (float)r.uz;
+  }
+  if (REDUCE) acc.add(r);
+  if (MACRO_ONLY) return;
+  if (PARITY == 0) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[(uint32_t)opp(q) * n + c] = St::ench(fv[q]);
+  } else if (__all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u)) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[c + kp.wr[q]] = St::ench(fv[q]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
+      f[c + (wall ? kp.pl[opp(q)] : kp.wr[q])] = St::ench(fv[q]);
+    }
+  }
+}
+
+__device__ __forceinline__ bool aa_live(const KParams& kp, uint32_t c, uint32_t fl) {
+  return !(fl & POG_CELL_SOLID) && c >= kp.guard_lo && c <= kp.guard_hi;
+}
+
+// One cell per thread (grid-stride when the grid is smaller than the lattice).
 template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
 __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
     const KParams kp, typename Store<S>::E* __restrict__ f, const uint32_t* __restrict__ flags,
@@ -42,61 +115,17 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
   using St = Store<S>;
   using C = typename St::C;
   const C rho0 = (C)kp.rho0;
-  const uint32_t n = kp.n;
   RedAcc<C> acc;
-  for (uint32_t c = blockIdx.x * AA_BLOCK + threadIdx.x; c < n; c += gridDim.x * AA_BLOCK) {
+  for (uint32_t c = blockIdx.x * AA_BLOCK + threadIdx.x; c < kp.n; c += gridDim.x * AA_BLOCK) {
     const uint32_t fl = flags[c];
-    if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
-    // every slot of cell c sits at fc + (a non-negative offset below 19 n) from the tables
-    typename St::E* const fc = f + c;
-    const bool open = (fl >> POG_LINK_SHIFT) == 0u;  // no solid neighbour
+    if (!aa_live(kp, c, fl)) continue;
+    typename St::E raw[19];
+    aa_load<S, PARITY>(kp, f, c, fl, raw);
     C fv[19];
-    if (PARITY == 0) {
 #pragma unroll
-      for (int q = 0; q < 19; ++q) fv[q] = St::ld(f, (uint32_t)q * n + c, q, rho0);
-    } else if (open) {
-#pragma unroll
-      for (int q = 0; q < 19; ++q) fv[q] = St::ld(fc, kp.rd[q], q, rho0);
-    } else {
-      // source c - e_q is the neighbour in direction opp(q); a solid one bounces f_q back
-#pragma unroll
-      for (int q = 0; q < 19; ++q) {
-        const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
-        fv[q] = St::ld(fc, wall ? kp.pl[q] : kp.rd[q], q, rho0);
-      }
-    }
-    C nu_st = (C)0;
-    if (!MACRO_ONLY && kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS))
-      nu_st = les_nu_stencil<C>(kp, c, u_prev);
-    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, pdrag, eps, nu_st);
-    if (rho_out) rho_out[c] = (float)r.rho;
-    if (u_out) {
-      u_out[c] = (float)r.ux;
-      u_out[n + c] = (float)r.uy;
-      u_out[2u * n + c] = (float)r.uz;
-    }
-    if (!MACRO_ONLY && u_next) {
-      u_next[c] = (float)r.ux;
-      u_next[n + c] = (float)r.uy;
-      u_next[2u * n + c] = (float)r.uz;
-    }
-    if (REDUCE) {
-      acc.add(r);
-    }
-    if (MACRO_ONLY) continue;
-    if (PARITY == 0) {
-#pragma unroll
-      for (int q = 0; q < 19; ++q) St::st(f, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
-    } else if (open) {
-#pragma unroll
-      for (int q = 0; q < 19; ++q) St::st(fc, kp.wr[q], q, fv[q], rho0);
-    } else {
-#pragma unroll
-      for (int q = 0; q < 19; ++q) {
-        const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
-        St::st(fc, wall ? kp.pl[opp(q)] : kp.wr[q], q, fv[q], rho0);
-      }
-    }
+    for (int q = 0; q < 19; ++q) fv[q] = St::dech(raw[q]);
+    aa_update<S, PARITY, REDUCE, MACRO_ONLY>(kp, f, c, fl, fv, force, pdrag, eps, u_prev, u_next, rho_out,
+                                             u_out, acc);
   }
   if (REDUCE) {
     double part[POG_RED_COUNT];
@@ -228,9 +257,9 @@ int launch_aa_tma(const KParams& kp, int parity, bool reduce, void* f, const uin
                   const float* force, const float* pdrag, const float* eps, const float* u_prev, float* u_next,
                   float* rho_out, float* u_out, double* red, cudaStream_t s);
 
-// Which step kernel pog_step uses: the register-staged one (default: measured faster on GB300
-// once bounce-back needs no neighbour loads) or the TMA-staged one (POG_AA_KERNEL=tma, needs a
-// 16-byte aligned distribution buffer; kept for A/B timing).
+// Which step kernel pog_step uses: the register-staged one (default: measured faster on GB300)
+// or the TMA-staged one (POG_AA_KERNEL=tma, needs a 16-byte aligned distribution buffer; kept
+// for A/B timing).  Both compute the same update.
 static bool use_tma(const void* f) {
   static int mode = -1;
   if (mode < 0) {
