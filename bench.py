@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="64^3 / 2,000 particles (profiling)")
     ap.add_argument("--precision-only", choices=["fp32", "fp16s", "bf16s"], default=None,
                     help="time only the 256^3 precision case in this storage for --steps steps (profiling)")
+    ap.add_argument("--precision-case", choices=["les_band", "plain"], default="les_band")
     return ap.parse_args()
 
 
@@ -193,11 +194,25 @@ class GraphOfSteps:
         self.s.t += self.n
 
 
-def precision_line(storage, steps, peak):
+PRECISION_CASES = {
+    # the 256^3 target case: D3Q19 + LES (local strain) + 3-cell porous band
+    "les_band": {},
+    # the plain 256^3 physics of the 64^3 case (no LES, no porous band)
+    "plain": {"les": False, "band": 0.0},
+}
+
+
+def precision_cfg(storage, case):
+    from pour_over_coffee_lbm_gb300.params import LES_LOCAL, LES_OFF, precision_256
+    kw = PRECISION_CASES[case]
+    return precision_256(storage=storage, les_mode=LES_LOCAL if kw.get("les", True) else LES_OFF,
+                         band=kw.get("band", 3.0))
+
+
+def precision_line(storage, steps, peak, case="les_band"):
     import torch
-    from pour_over_coffee_lbm_gb300.params import precision_256
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
-    cfg = precision_256(storage=storage)
+    cfg = precision_cfg(storage, case)
     s = GB300LBMSolver(cfg)
     for _ in range(4):
         s.run(1)
@@ -231,32 +246,40 @@ def precision_line(storage, steps, peak):
     return out
 
 
-def precision_errors(steps):
+def precision_errors(steps, case="les_band"):
     """u and rho relative L2 error (fluid cells) of FP32 / FP16S / BF16S storage against an FP64
-    run of the same 256^3 case from the same initial state after `steps` steps."""
+    run of the same 256^3 case from the same initial state, after 500, 1000, ... `steps` steps."""
     import torch
-    from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32, STORE_F64, precision_256
+    from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32, STORE_F64
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
-    ref = GB300LBMSolver(precision_256(storage=STORE_F64))
-    ref.run(steps - 1)
-    ref.run(1, want_macro=True)
-    fluid = (ref.flags & 1) == 0
-    u64 = ref._u[:, fluid].double().clone()
-    r64 = ref._rho[fluid].double().clone()
-    del ref
-    torch.cuda.empty_cache()
-    out = {"steps": steps}
-    for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
-        s = GB300LBMSolver(precision_256(storage=st))
-        s.run(steps - 1)
-        s.run(1, want_macro=True)
-        u = s._u[:, fluid].double()
-        r = s._rho[fluid].double()
-        out[name] = {"u_rel_l2": float(torch.linalg.norm(u - u64) / torch.linalg.norm(u64)),
-                     "rho_rel_l2": float(torch.linalg.norm(r - r64) / torch.linalg.norm(r64))}
+    checks = sorted({c for c in (500, 1000, steps) if c <= steps})
+
+    def trajectory(st):
+        s = GB300LBMSolver(precision_cfg(st, case))
+        done, out = 0, {}
+        for c in checks:
+            s.run(c - done - 1)
+            s.run(1, want_macro=True)
+            done = c
+            out[c] = (s._u.double().clone(), s._rho.double().clone())
+        fluid = (s.flags & 1) == 0
         del s
         torch.cuda.empty_cache()
-    return out
+        return out, fluid
+
+    ref, fluid = trajectory(STORE_F64)
+    res = {"steps": checks}
+    for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
+        got, _ = trajectory(st)
+        res[name] = {"u_rel_l2": [], "rho_rel_l2": []}
+        for c in checks:
+            u, r = got[c]
+            u64, r64 = ref[c]
+            res[name]["u_rel_l2"].append(float(torch.linalg.norm((u - u64)[:, fluid]) / torch.linalg.norm(u64[:, fluid])))
+            res[name]["rho_rel_l2"].append(float(torch.linalg.norm((r - r64)[fluid]) / torch.linalg.norm(r64[fluid])))
+        del got
+        torch.cuda.empty_cache()
+    return res
 
 
 def cpu_baseline(cfg, pc, seconds):
@@ -382,14 +405,16 @@ def run_ours(args):
         from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
         del graph
         torch.cuda.empty_cache()
-        p32 = precision_line(STORE_F32, 200, peak)
-        p16 = precision_line(STORE_F16S, 200, peak)
-        pb16 = precision_line(STORE_BF16S, 200, peak)
-        errs = precision_errors(args.error_steps)
-        extra = {"workload": "256^3 D3Q19 + LES(local) + porous band, no particles",
-                 "fp32": p32, "fp16s": p16, "bf16s": pb16, "error_vs_fp64": errs,
-                 "fp16s_vs_fp32_mlups": round(p16["mlups"] / p32["mlups"], 3),
-                 "bf16s_vs_fp32_mlups": round(pb16["mlups"] / p32["mlups"], 3)}
+        extra = {}
+        for case, label in (("les_band", "256^3 D3Q19 + LES(local) + porous band, no particles"),
+                            ("plain", "256^3 D3Q19, gravity + inlet/outlet + cone walls (no LES, no band)")):
+            p32 = precision_line(STORE_F32, 200, peak, case)
+            p16 = precision_line(STORE_F16S, 200, peak, case)
+            pb16 = precision_line(STORE_BF16S, 200, peak, case)
+            errs = precision_errors(args.error_steps, case) if args.error_steps > 0 else None
+            extra[case] = {"workload": label, "fp32": p32, "fp16s": p16, "bf16s": pb16, "error_vs_fp64": errs,
+                           "fp16s_vs_fp32_mlups": round(p16["mlups"] / p32["mlups"], 3),
+                           "bf16s_vs_fp32_mlups": round(pb16["mlups"] / p32["mlups"], 3)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -484,7 +509,7 @@ def run_precision_only(args):
     from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
     torch.cuda.set_device(0)
     st = {"fp32": STORE_F32, "fp16s": STORE_F16S, "bf16s": STORE_BF16S}[args.precision_only]
-    out = precision_line(st, max(GRAPH_STEPS, args.steps), peaks())
+    out = precision_line(st, max(GRAPH_STEPS, args.steps), peaks(), args.precision_case)
     print(json.dumps({"precision_only": args.precision_only, **out}), flush=True)
 
 

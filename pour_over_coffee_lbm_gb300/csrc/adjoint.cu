@@ -92,8 +92,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
       ls[q] = wall ? (C)lam_next[(uint32_t)opp(q) * n + c] : (C)lam_next[(uint32_t)q * n + dst];
     }
     C f[19];
+    const C rs = (C)kp.rho0;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[q] = (C)ft[(uint32_t)q * n + c];
+    for (int q = 0; q < 19; ++q) f[q] = St::ld(ft, (uint32_t)q * n + c, q, rs);
     C rho = 0, mx = 0, my = 0, mz = 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {

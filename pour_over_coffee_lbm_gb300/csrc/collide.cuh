@@ -58,6 +58,14 @@ __host__ __device__ __forceinline__ C feq_q(int q, C rho, C ux, C uy, C uz, C us
   return (C)wd(q) * rho * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - usq15);
 }
 
+// f_eq_q - w_q rs for a density rr = rs + dr, without forming f_eq_q: w_q (dr + rr (3 e.u +
+// 4.5 (e.u)^2 - 1.5 u.u)).
+template <typename C>
+__host__ __device__ __forceinline__ C feq_dev_q(int q, C rr, C dr, C ux, C uy, C uz, C usq15) {
+  C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
+  return (C)wd(q) * (dr + rr * ((C)3 * eu + (C)4.5 * eu * eu - usq15));
+}
+
 // One direction pair (q, opp q) of the BGK + Guo collision, q with e = (ex, ey, ez), written as
 // a chain of FMAs.  Per weight class w (a1 = omega w rho, b3 = 3 (1 - omega/2) w):
 //   omega f_eq + S, even in e:  sym  = A + (e.u)(B e.u + Cc e.F),  A = a1 (1 - 1.5 u.u) - b3 u.F,
@@ -91,10 +99,35 @@ __host__ __device__ __forceinline__ void collide_pair(C f[19], C ux, C uy, C uz,
   f[P] = fma(keep, fp, sym - asym);
 }
 
+// Two direction pairs (Q1, Q2) of one weight class at once, in Blackwell's packed FP32x2
+// arithmetic (FFMA2/FADD2/FMUL2: two FP32 lanes per instruction, each lane rounded as its
+// scalar counterpart).  Same update as collide_pair.
+template <int Q1, int Q2, typename C>
+__device__ __forceinline__ void collide_pair2(C f[19], C ux, C uy, C uz, C Fx, C Fy, C Fz, C keep,
+                                              const PairCoef<C>& k) {
+  static_assert(sizeof(C) == 4, "packed pairs are FP32");
+  constexpr int P1 = opp(Q1), P2 = opp(Q2);
+  const float2 EU = make_float2((C)cx(Q1) * ux + (C)cy(Q1) * uy + (C)cz(Q1) * uz,
+                                (C)cx(Q2) * ux + (C)cy(Q2) * uy + (C)cz(Q2) * uz);
+  const float2 EF = make_float2((C)cx(Q1) * Fx + (C)cy(Q1) * Fy + (C)cz(Q1) * Fz,
+                                (C)cx(Q2) * Fx + (C)cy(Q2) * Fy + (C)cz(Q2) * Fz);
+  const float2 A = make_float2(k.A, k.A), B = make_float2(k.B, k.B), Cc = make_float2(k.Cc, k.Cc);
+  const float2 D = make_float2(k.D, k.D), b3 = make_float2(k.b3, k.b3), K = make_float2(keep, keep);
+  const float2 sym = __ffma2_rn(EU, __ffma2_rn(Cc, EF, __fmul2_rn(B, EU)), A);
+  const float2 asym = __ffma2_rn(D, EU, __fmul2_rn(b3, EF));
+  const float2 FQ = __ffma2_rn(K, make_float2(f[Q1], f[Q2]), __fadd2_rn(sym, asym));
+  const float2 FP = __ffma2_rn(K, make_float2(f[P1], f[P2]), __ffma2_rn(asym, make_float2(-1.0f, -1.0f), sym));
+  f[Q1] = FQ.x;
+  f[Q2] = FQ.y;
+  f[P1] = FP.x;
+  f[P2] = FP.y;
+}
+
 // f[19]: incoming populations on entry, post-collision populations on exit.
-// SH (shifted): f holds h_q = (f_q - w_q rho0) / sc instead of f_q, in and out -- the form the
-// 16-bit storages keep.  Moments, Pi_neq and the post-collision update are rewritten for h (the
-// shift and scale fold into per-cell coefficients), so no population is ever converted back.
+// SH (shifted): f holds h_q = (f_q - w_q rs) / sc instead of f_q, in and out -- the form the
+// shifted storages keep, rs = the cell's shift density.  Moments, Pi_neq and the post-collision
+// update are rewritten for h (the shift and scale fold into per-cell coefficients), so no
+// population is ever converted back.
 // nu_st: nu_sgs from the velocity stencil (LES_STENCIL mode), computed by the caller.
 // pdrag: [4][n] particle drag deposit (Kp = sum w beta, Kv = sum w beta v_p) or null; the
 // particle force on the fluid, Kv - Kp u, is taken implicitly in u (stable at any loading).
@@ -103,9 +136,9 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
                                                                C f[19], const float* __restrict__ force,
                                                                const float* __restrict__ pdrag,
                                                                const float* __restrict__ eps, C nu_st,
-                                                               C sc = (C)1) {
+                                                               C sc = (C)1, C rs = (C)0) {
   CellResult<C> res;
-  const C rho0 = (C)kp.rho0;
+  const C rho0 = rs;  // shift density (SH only)
   // ---- moments from one sweep of adds (of h when SH: sum w = 1, sum w e = 0, sum w e e = I/3) --
   const C sx = f[1] + f[2], sy = f[3] + f[4], sz = f[5] + f[6];
   const C sxy = (f[7] + f[8]) + (f[9] + f[10]);
@@ -115,7 +148,9 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   const C mxs = (f[1] - f[2]) + ((f[7] - f[8]) + (f[9] - f[10])) + ((f[11] - f[12]) + (f[13] - f[14]));
   const C mys = (f[3] - f[4]) + ((f[7] + f[8]) - (f[9] + f[10])) + ((f[15] - f[16]) + (f[17] - f[18]));
   const C mzs = (f[5] - f[6]) + ((f[11] + f[12]) - (f[13] + f[14])) + ((f[15] + f[16]) - (f[17] + f[18]));
-  const C rho = SH ? fma(sc, rsum, rho0) : rsum;
+  // SH: drho = rho - rs straight from the deviations (no cancellation against rs)
+  const C drho = SH ? sc * rsum : (C)0;
+  const C rho = SH ? rho0 + drho : rsum;
   const C mx = SH ? sc * mxs : mxs, my = SH ? sc * mys : mys, mz = SH ? sc * mzs : mzs;
   const C inv_sc = SH ? (C)1 / sc : (C)1;
   res.outflow = (C)0;
@@ -134,11 +169,11 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
       res.outflow = -mz;
     }
     C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
+    // SH: f_eq - w rs = w ((rr - rs) + rr (3 e.u + 4.5 (e.u)^2 - 1.5 u.u)), rr - rs exact
+    const C dr = SH ? ((fl & POG_CELL_INLET) ? drho : rr - rho0) : (C)0;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) {
-      const C fe = feq_q<C>(q, rr, ux, uy, uz, usq15);
-      f[q] = SH ? (fe - (C)wd(q) * rho0) * inv_sc : fe;
-    }
+    for (int q = 0; q < 19; ++q) f[q] = SH ? feq_dev_q<C>(q, rr, dr, ux, uy, uz, usq15) * inv_sc
+                                           : feq_q<C>(q, rr, ux, uy, uz, usq15);
     res.rho = rho;
     res.ux = ux;
     res.uy = uy;
@@ -230,7 +265,7 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   if (kp.les_mode == POG_LES_LOCAL && !porous) {
     // Pi_neq = sum e e f - rho (u u + I/3)
     // SH: sum e_a e_b f = rho0/3 delta_ab + sc sum e_a e_b h
-    const C r3 = (SH ? rho - rho0 : rho) * (C)(1.0 / 3.0);
+    const C r3 = (SH ? drho : rho) * (C)(1.0 / 3.0);
     const C m2 = SH ? sc : (C)1;
     const C Pxx = m2 * (sx + sxy + sxz) - (rho * ux * ux + r3);
     const C Pyy = m2 * (sy + sxy + syz) - (rho * uy * uy + r3);
@@ -256,34 +291,37 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   if (kp.forcing_mode == POG_FORCING_GUO) {
     const C A = (C)1 - (C)0.5 * omega;
     const C uF = ux * Fx + uy * Fy + uz * Fz;
-    const C base = (C)1 - (C)1.5 * usq;
+    // SH: h* = keep h + (omega f_eq + S - omega w rs) / sc.  The shift joins the even part as
+    // base = (rho - rs)/rho - 1.5 u.u (omega w rho (1 - 1.5 u.u) - omega w rs), with rho - rs
+    // taken from the deviation sum, and 1/sc scales the two per-cell factors omega rho and A, so
+    // every coefficient below carries both.
+    const C base = SH ? drho * inv_rho - (C)1.5 * usq : (C)1 - (C)1.5 * usq;
+    const C or_ = SH ? omega * rho * inv_sc : omega * rho;
+    const C As = SH ? A * inv_sc : A;
     // weight classes: w0 = 1/3 (rest), w1 = 1/18 (axes), w2 = 1/36 (edges)
-    const C or_ = omega * rho;
     const C a1_0 = or_ * (C)(1.0 / 3.0), a1_1 = or_ * (C)(1.0 / 18.0), a1_2 = or_ * (C)(1.0 / 36.0);
-    const C b3_0 = A, b3_1 = A * (C)(3.0 / 18.0), b3_2 = A * (C)(3.0 / 36.0);
+    const C b3_0 = As, b3_1 = As * (C)(3.0 / 18.0), b3_2 = As * (C)(3.0 / 36.0);
     // rest population: f0* = keep f0 + omega w0 rho base - 3 A w0 uF
-    PairCoef<C> k1 = pair_coef<C>(a1_1, b3_1, uF, base), k2 = pair_coef<C>(a1_2, b3_2, uF, base);
-    if (SH) {
-      // h* = keep h + (omega f_eq + S - omega w rho0) / sc: subtract omega w rho0 from the even
-      // part and scale every coefficient by 1/sc
-      const C or0 = omega * rho0;
-      f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF - or0 * (C)(1.0 / 3.0)) * inv_sc;
-      k1.A = (k1.A - or0 * (C)(1.0 / 18.0)) * inv_sc;
-      k2.A = (k2.A - or0 * (C)(1.0 / 36.0)) * inv_sc;
-      k1.B *= inv_sc; k1.Cc *= inv_sc; k1.D *= inv_sc; k1.b3 *= inv_sc;
-      k2.B *= inv_sc; k2.Cc *= inv_sc; k2.D *= inv_sc; k2.b3 *= inv_sc;
+    f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF);
+    const PairCoef<C> k1 = pair_coef<C>(a1_1, b3_1, uF, base), k2 = pair_coef<C>(a1_2, b3_2, uF, base);
+    if constexpr (sizeof(C) == 4) {
+      // FP32: eight of the nine pairs two at a time in packed FP32x2 arithmetic
+      collide_pair2<1, 3>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+      collide_pair<5, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+      collide_pair2<7, 8>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair2<11, 12>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair2<15, 16>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
     } else {
-      f[0] = keep * f[0] + (a1_0 * base - b3_0 * uF);
+      collide_pair<1, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+      collide_pair<3, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+      collide_pair<5, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
+      collide_pair<7, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair<8, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair<11, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair<12, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair<15, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
+      collide_pair<16, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
     }
-    collide_pair<1, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
-    collide_pair<3, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
-    collide_pair<5, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k1);
-    collide_pair<7, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
-    collide_pair<8, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
-    collide_pair<11, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
-    collide_pair<12, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
-    collide_pair<15, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
-    collide_pair<16, C>(f, ux, uy, uz, Fx, Fy, Fz, keep, k2);
   } else {
     const C usq15 = (C)1.5 * usq;
     C taus = tau < (C)0.6 ? (C)0.6 : (tau > (C)1.5 ? (C)1.5 : tau);
@@ -306,7 +344,7 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
       }
       const C fe = feq_q<C>(q, rho, ux, uy, uz, usq15);
       if (SH) {
-        const C he = (fe - (C)wd(q) * rho0) * inv_sc;
+        const C he = feq_dev_q<C>(q, rho, drho, ux, uy, uz, usq15) * inv_sc;
         f[q] = he + keep * (f[q] - he) + S * inv_sc;
       } else {
         f[q] = fe + keep * (f[q] - fe) + S;
@@ -346,16 +384,19 @@ __host__ __device__ __forceinline__ C les_nu_stencil(const KParams& kp, uint32_t
 // ---- storage formats ------------------------------------------------------------------------
 template <int S>
 struct Store;
-// dec/enc convert between a stored value and f_q; dech/ench between a stored value and the form
-// collide_cell<C, SHIFTED> works on (f_q itself, or h_q = (f_q - w_q rho0) / SCALE when SHIFTED).
+// dec/enc convert between a stored value and f_q (rs = the shift density of the slot's cell);
+// dech/ench between a stored value and the form collide_cell<C, SHIFTED> works on (h_q =
+// (f_q - w_q rs) / SCALE when SHIFTED, else f_q).  FP32 stores the shifted form (scale 1): f_q of
+// a slow flow is w_q rs plus a small deviation, and keeping only the deviation keeps its digits.
+// FP64 (the reference storage) stores f_q.
 template <>
 struct Store<POG_STORE_F32> {
   using E = float;
   using C = float;
-  static constexpr bool SHIFTED = false;
+  static constexpr bool SHIFTED = true;
   static constexpr float SCALE = 1.0f;
-  __device__ static __forceinline__ C dec(E v, int, C) { return v; }
-  __device__ static __forceinline__ E enc(C v, int, C) { return v; }
+  __device__ static __forceinline__ C dec(E v, int q, C rs) { return __fadd_rn(v, __fmul_rn((float)wd(q), rs)); }
+  __device__ static __forceinline__ E enc(C v, int q, C rs) { return __fsub_rn(v, __fmul_rn((float)wd(q), rs)); }
   __device__ static __forceinline__ C dech(E v) { return v; }
   __device__ static __forceinline__ E ench(C v) { return v; }
   __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C r) { return dec(p[i], q, r); }
@@ -374,9 +415,9 @@ struct Store<POG_STORE_F64> {
   __device__ static __forceinline__ C ld(const E* p, uint32_t i, int q, C r) { return dec(p[i], q, r); }
   __device__ static __forceinline__ void st(E* p, uint32_t i, int q, C v, C r) { p[i] = enc(v, q, r); }
 };
-// 16-bit storages hold the shifted form h = (f - w_q rho0) / SCALE (FP16: SCALE = 2^-12 keeps
+// 16-bit storages hold the shifted form h = (f - w_q rs) / SCALE (FP16: SCALE = 2^-12 keeps
 // small deviations normal; BF16: SCALE = 1).  dec is one rounding of w + h SCALE and enc rounds
-// (f - w) / SCALE once before the 16-bit rounding, w = fl(w_q rho0): the same roundings, in the
+// (f - w) / SCALE once before the 16-bit rounding, w = fl(w_q rs): the same roundings, in the
 // same order, as the oracle's storage emulation.  The step kernel skips dec/enc altogether and
 // collides h directly (dech/ench are the bare 16-bit conversions).
 template <>

@@ -34,16 +34,16 @@ constexpr int AA_BLOCK = 256;
 #endif
 
 // The 19 incoming populations of cell c as stored values (AA read pattern of PARITY).  Every
-// slot of cell c is element c + (a non-negative offset below 19 n) of the offset tables.  The odd
-// step takes the streaming offsets alone when no cell of the warp touches a solid neighbour (one
-// warp-uniform test); otherwise each direction chooses its streamed or bounced slot.
+// slot of cell c is element c + (a non-negative offset below 19 n) of the offset tables.  On the
+// odd step, `open` (warp-uniform: no cell of the warp touches a solid neighbour) selects the plain
+// streaming offsets; otherwise each direction chooses its streamed or bounced slot.
 template <int S, int PARITY>
 __device__ __forceinline__ void aa_load(const KParams& kp, const typename Store<S>::E* __restrict__ f,
-                                        uint32_t c, uint32_t fl, typename Store<S>::E raw[19]) {
+                                        uint32_t c, uint32_t fl, bool open, typename Store<S>::E raw[19]) {
   if (PARITY == 0) {
 #pragma unroll
     for (int q = 0; q < 19; ++q) raw[q] = f[(uint32_t)q * kp.n + c];
-  } else if (__all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u)) {
+  } else if (open) {
 #pragma unroll
     for (int q = 0; q < 19; ++q) raw[q] = f[c + kp.rd[q]];
   } else {
@@ -56,23 +56,24 @@ __device__ __forceinline__ void aa_load(const KParams& kp, const typename Store<
   }
 }
 
-// Collision of cell c (populations fv), its macroscopic outputs and sums, and the AA stores of
-// the post-collision populations (MACRO_ONLY: outputs only).
+// Collision of cell c (populations fv in the storage's collision form), its macroscopic outputs
+// and sums, and the AA stores of the post-collision populations (MACRO_ONLY: outputs only).
 template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
 __device__ __forceinline__ void aa_update(const KParams& kp, typename Store<S>::E* __restrict__ f,
-                                          uint32_t c, uint32_t fl, typename Store<S>::C fv[19],
+                                          uint32_t c, uint32_t fl, bool open, typename Store<S>::C fv[19],
                                           const float* __restrict__ force, const float* __restrict__ pdrag,
                                           const float* __restrict__ eps, const float* __restrict__ u_prev,
                                           float* __restrict__ u_next, float* __restrict__ rho_out,
                                           float* __restrict__ u_out, RedAcc<typename Store<S>::C>& acc) {
   using St = Store<S>;
   using C = typename St::C;
-  const C rho0 = (C)kp.rho0;
   const uint32_t n = kp.n;
   C nu_st = (C)0;
   if (!MACRO_ONLY && kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS))
     nu_st = les_nu_stencil<C>(kp, c, u_prev);
-  const CellResult<C> r = collide_cell<C, St::SHIFTED>(kp, fl, c, fv, force, pdrag, eps, nu_st, (C)St::SCALE);
+  const C rs = (C)kp.rho0;  // shift density of the shifted storages
+  const CellResult<C> r =
+      collide_cell<C, St::SHIFTED>(kp, fl, c, fv, force, pdrag, eps, nu_st, (C)St::SCALE, rs);
   if (rho_out) rho_out[c] = (float)r.rho;
   if (u_out) {
     u_out[c] = (float)r.ux;
@@ -89,7 +90,9 @@ __device__ __forceinline__ void aa_update(const KParams& kp, typename Store<S>::
   if (PARITY == 0) {
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[(uint32_t)opp(q) * n + c] = St::ench(fv[q]);
-  } else if (__all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u)) {
+    return;
+  }
+  if (open) {
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[c + kp.wr[q]] = St::ench(fv[q]);
   } else {
@@ -114,18 +117,18 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
     float* __restrict__ u_out, double* __restrict__ red) {
   using St = Store<S>;
   using C = typename St::C;
-  const C rho0 = (C)kp.rho0;
   RedAcc<C> acc;
   for (uint32_t c = blockIdx.x * AA_BLOCK + threadIdx.x; c < kp.n; c += gridDim.x * AA_BLOCK) {
     const uint32_t fl = flags[c];
     if (!aa_live(kp, c, fl)) continue;
+    const bool open = PARITY == 1 && __all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u);
     typename St::E raw[19];
-    aa_load<S, PARITY>(kp, f, c, fl, raw);
+    aa_load<S, PARITY>(kp, f, c, fl, open, raw);
     C fv[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) fv[q] = St::dech(raw[q]);
-    aa_update<S, PARITY, REDUCE, MACRO_ONLY>(kp, f, c, fl, fv, force, pdrag, eps, u_prev, u_next, rho_out,
-                                             u_out, acc);
+    aa_update<S, PARITY, REDUCE, MACRO_ONLY>(kp, f, c, fl, open, fv, force, pdrag, eps, u_prev, u_next,
+                                             rho_out, u_out, acc);
   }
   if (REDUCE) {
     double part[POG_RED_COUNT];

@@ -17,15 +17,15 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
     double* __restrict__ red) {
   using St = Store<S>;
   using C = typename St::C;
-  const C rho0 = (C)kp.rho0;
   const uint32_t n = kp.n;
   RedAcc<C> acc;
   for (uint32_t c = blockIdx.x * PUSH_BLOCK + threadIdx.x; c < n; c += gridDim.x * PUSH_BLOCK) {
     const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
+    const C rs = (C)kp.rho0;  // shift density of the shifted storages
     C fv[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) fv[q] = St::ld(fin, (uint32_t)q * n + c, q, rho0);
+    for (int q = 0; q < 19; ++q) fv[q] = St::ld(fin, (uint32_t)q * n + c, q, rs);
     C nu_st = (C)0;
     if (kp.les_mode == POG_LES_STENCIL && u_prev && !(fl & POG_CELL_POROUS))
       nu_st = les_nu_stencil<C>(kp, c, u_prev);
@@ -44,9 +44,9 @@ __global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
       const uint32_t dst = c + (uint32_t)kp.off[q];
       const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
       if (wall)
-        St::st(fout, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
+        St::st(fout, (uint32_t)opp(q) * n + c, q, fv[q], rs);
       else
-        St::st(fout, (uint32_t)q * n + dst, q, fv[q], rho0);
+        St::st(fout, (uint32_t)q * n + dst, q, fv[q], rs);
     }
   }
   if (REDUCE) {

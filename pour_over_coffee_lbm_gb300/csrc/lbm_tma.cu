@@ -159,7 +159,6 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
     }
   } else {
     // ---------------- consumers ----------------
-    const C rho0 = (C)kp.rho0;
     const uint32_t lo = kp.guard_lo, hi = kp.guard_hi;
     for (uint32_t it = 0; it < nit; ++it) {
       const int stage = (int)(it % Cfg::STAGES);
@@ -172,10 +171,12 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
       const int* sl = leads + stage * 20;
       const bool live = c <= hi && c >= lo;
       const uint32_t fl = live ? flags[c] : POG_CELL_SOLID;
+      const C rs = (C)kp.rho0;  // shift density of the shifted storages
       C fv[19];
       if (!(fl & POG_CELL_SOLID)) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) fv[q] = St::ld(sb + q * Cfg::PLANE, (uint32_t)(sl[q] + (int)tid), q, rho0);
+        for (int q = 0; q < 19; ++q)
+          fv[q] = St::ld(sb + q * Cfg::PLANE, (uint32_t)(sl[q] + (int)tid), q, rs);
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[stage]);  // the stage's values are in registers
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
       if (PARITY == 1 && (fl & POG_CELL_NEAR_SOLID)) {
 #pragma unroll
         for (int q = 1; q < 19; ++q)
-          if ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u) fv[q] = St::ld(f, (uint32_t)q * n + c, q, rho0);
+          if ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u) fv[q] = St::ld(f, (uint32_t)q * n + c, q, rs);
       }
       C nu_st = (C)0;
       if (kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS)) nu_st = les_nu_stencil<C>(kp, c, u_prev);
@@ -204,13 +205,13 @@ __global__ void __launch_bounds__(CTA_THREADS, TmaCfg<S>::MIN_BLOCKS) aa_tma_ker
       }
       if (PARITY == 0) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) St::st(f, (uint32_t)opp(q) * n + c, q, fv[q], rho0);
+        for (int q = 0; q < 19; ++q) St::st(f, (uint32_t)opp(q) * n + c, q, fv[q], rs);
       } else {
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
           const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
           const uint32_t idx = wall ? (uint32_t)opp(q) * n + c : (uint32_t)q * n + (c + (uint32_t)kp.off[q]);
-          St::st(f, idx, q, fv[q], rho0);
+          St::st(f, idx, q, fv[q], rs);
         }
       }
     }
