@@ -56,11 +56,13 @@ extern "C" {
 
 /* ---- enums -------------------------------------------------------------------------------- */
 enum pog_storage {     /* how the distributions are stored in HBM                           */
-  POG_STORE_F32 = 0,   /* float f_i                                                          */
-  POG_STORE_F16S = 1,  /* IEEE half of (f_i - w_i*rho0); collision in FP32                   */
+  POG_STORE_F32 = 0,   /* float (f_i - w_i*rho0); collision in FP32 on the deviations        */
+  POG_STORE_F16S = 1,  /* IEEE half of (f_i - w_i*rho0)*2^12; collision in FP32              */
   POG_STORE_BF16S = 2, /* bfloat16 of (f_i - w_i*rho0); collision in FP32                    */
   POG_STORE_F64 = 3    /* double f_i, collision in FP64 (reference runs for error reports)  */
 };
+/* The stored form is internal: pog_export_natural / pog_import_natural convert to and from
+ * plain f_i in FP32 or FP64 for every storage. */
 enum pog_les_mode {
   POG_LES_OFF = 0,
   POG_LES_STENCIL = 1, /* |S| by central differences of the previous step's u
@@ -153,7 +155,8 @@ long long pog_launch_count(int reset);
 int pog_validate_params(const pog_params* p);
 
 /* ---- geometry ------------------------------------------------------------------------------ */
-/* Build the uint8 cell flags of the V60 mask, drain hole, inlet/outlet disks and porous band.
+/* Build the cell flag words (own flags + the 18 solid-neighbour link bits) of the V60 mask,
+ * drain hole, inlet/outlet disks and porous band: flags[c], c = (k*ny + j)*nx + i.
  * Replaces FilterPaperSystem._setup_v60_geometry / _setup_filter_zones
  * (filter_paper.py:206-364) and the LES mask copy (filter_paper.py:199-204).  Computed in FP64
  * without contraction: the result is bit-exact with the CPU restatement. */
