@@ -1,0 +1,244 @@
+"""z-slab decomposition of the AA-pattern lattice (the reference's only multi-GPU strategy splits
+the domain along z the same way: src/core/cuda_dual_gpu_lbm.py:67-76).
+
+Slab s owns planes [z0, z1) and holds them between two ghost planes, (z1 - z0 + 2) planes in all,
+ghost-below | owned | ghost-above.  The step kernel never updates the ghost planes (they fall
+outside its one-plane guard), so a slab runs pog_step unchanged on its own buffer.
+
+Only the odd AA step crosses an interface, and across the interface between slab s (below) and
+s+1 (above) it touches exactly the slots of the five directions with c_z = -1 (DOWN) on the lower
+side and the five with c_z = +1 (UP) on the upper side, each read and then written by the same
+cell.  So one odd step needs:
+
+  before:  ghost_below(s+1)[DOWN] <- top_owned(s)[DOWN]
+           ghost_above(s)[UP]     <- bottom_owned(s+1)[UP]
+  after:   top_owned(s)[DOWN]     <- ghost_below(s+1)[DOWN]   where the slot's writer is fluid
+           bottom_owned(s+1)[UP]  <- ghost_above(s)[UP]       where the slot's writer is fluid
+
+The writer of slot (x, q), q in DOWN, is the cell x - e_q on the upper slab's first plane; when it
+is solid, x itself may have bounced f into that slot on its own side, so the copy-back is masked
+(`writer_masks`).  The even step is local.  An interface moves five population planes each way
+before and again after every odd step (320 x 320 FP16: 1.0 MB per face and direction).
+
+`SlabLattice` runs all slabs on one GPU with device-local copies (bit-identical to the undivided
+lattice: the kernel computes every cell from the same inputs).  `RankHalo` is the same protocol
+between processes over torch.distributed point-to-point messages (one slab per rank).
+"""
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from .params import CELL_SOLID, LES_STENCIL, LatticeConfig, RED_COUNT
+from .solver import CX, CY, CZ, _STORAGE_DTYPE
+
+UP = [q for q in range(19) if CZ[q] == 1]     # 5, 11, 12, 15, 16
+DOWN = [q for q in range(19) if CZ[q] == -1]  # 6, 13, 14, 17, 18
+
+
+def slab_bounds(nz: int, nslabs: int) -> List[Tuple[int, int]]:
+    """Balanced [z0, z1) per slab."""
+    if not 1 <= nslabs <= nz // 2:
+        raise ValueError("nslabs must be in [1, nz/2]")
+    cuts = [s * nz // nslabs for s in range(nslabs + 1)]
+    return [(cuts[s], cuts[s + 1]) for s in range(nslabs)]
+
+
+def slab_flags(flags: np.ndarray, z0: int, z1: int) -> np.ndarray:
+    """Flag words of planes z0-1 .. z1 of a [nz, ny, nx] array, out-of-domain ghost planes solid."""
+    nz = flags.shape[0]
+    out = np.full((z1 - z0 + 2,) + flags.shape[1:], CELL_SOLID, dtype=flags.dtype)
+    lo, hi = max(z0 - 1, 0), min(z1 + 1, nz)
+    out[lo - (z0 - 1): hi - (z0 - 1)] = flags[lo:hi]
+    return out
+
+
+def writer_masks(writer_plane_flags: np.ndarray, slots: Sequence[int]) -> np.ndarray:
+    """[len(slots), ny, nx] bool: slot (x, q) of the interface plane is written by the fluid cell
+    x - e_q of the neighbouring plane, whose flag words are `writer_plane_flags` [ny, nx]."""
+    fluid = (writer_plane_flags & CELL_SOLID) == 0
+    ny, nx = fluid.shape
+    out = np.zeros((len(slots), ny, nx), dtype=bool)
+    for a, q in enumerate(slots):
+        # mask[j, i] = fluid[j - cy, i - cx] (False outside the plane)
+        sy, sx = int(CY[q]), int(CX[q])
+        dst = out[a, max(sy, 0): ny + min(sy, 0), max(sx, 0): nx + min(sx, 0)]
+        dst[...] = fluid[max(-sy, 0): ny + min(-sy, 0), max(-sx, 0): nx + min(-sx, 0)]
+    return out
+
+
+class SlabLattice:
+    """One lattice split into z-slabs on one GPU, each slab a separate distribution buffer driven
+    through pog_step, with device-local halo copies around every odd step."""
+
+    def __init__(self, cfg: LatticeConfig, nslabs: int, flags: Optional[np.ndarray] = None,
+                 device: str = "cuda"):
+        if cfg.les_mode == LES_STENCIL:
+            raise ValueError("slab decomposition supports les_mode OFF or LOCAL (no u halo)")
+        self.lib = _lib.load()
+        self.cfg = cfg
+        self.device = torch.device(device)
+        dev = self.device
+        shape = (cfg.nz, cfg.ny, cfg.nx)
+        if flags is None:
+            p = cfg.to_c()
+            g = torch.empty(shape, dtype=torch.int32, device=dev)
+            _lib.check(self.lib.pog_build_flags(p, _lib.ptr(g), _lib.stream_handle()))
+            flags = g.cpu().numpy()
+        flags = np.asarray(flags).astype(np.int32).reshape(shape)
+        self.global_flags = flags
+        self.bounds = slab_bounds(cfg.nz, nslabs)
+        self.slabs = []
+        for z0, z1 in self.bounds:
+            sc = cfg.replace(nz=z1 - z0 + 2)
+            p = sc.to_c()
+            _lib.check(self.lib.pog_validate_params(p))
+            fl = torch.as_tensor(slab_flags(flags, z0, z1)).to(dev)
+            f = torch.empty((19, z1 - z0 + 2, cfg.ny, cfg.nx), dtype=_STORAGE_DTYPE[cfg.storage], device=dev)
+            self.slabs.append({"z0": z0, "z1": z1, "cfg": sc, "p": p, "flags": fl, "f": f,
+                               "rho": torch.zeros((z1 - z0 + 2, cfg.ny, cfg.nx), dtype=torch.float32, device=dev),
+                               "u": torch.zeros((3, z1 - z0 + 2, cfg.ny, cfg.nx), dtype=torch.float32, device=dev)})
+        # copy-back masks per interface: DOWN slots of the lower slab's top plane are written by
+        # the upper slab's first plane, UP slots of the upper slab's first plane by the lower top
+        self.masks = []
+        for s in range(nslabs - 1):
+            lo, up = self.slabs[s], self.slabs[s + 1]
+            m_down = writer_masks(flags[up["z0"]], DOWN)
+            m_up = writer_masks(flags[lo["z1"] - 1], UP)
+            self.masks.append((torch.as_tensor(m_down).to(dev), torch.as_tensor(m_up).to(dev)))
+        self.down = torch.as_tensor(DOWN, device=dev)
+        self.up = torch.as_tensor(UP, device=dev)
+        self.red = torch.zeros(RED_COUNT, dtype=torch.float64, device=dev)
+        self.t = 0
+        self._in_done = False
+        self.init_equilibrium(cfg.rho0)
+
+    def _s(self):
+        return _lib.stream_handle()
+
+    def init_equilibrium(self, rho0: float, u0=(0.0, 0.0, 0.0)):
+        for sl in self.slabs:
+            _lib.check(self.lib.pog_init_equilibrium(sl["p"], _lib.ptr(sl["f"]), _lib.ptr(sl["flags"]),
+                                                     float(rho0), float(u0[0]), float(u0[1]), float(u0[2]),
+                                                     self._s()))
+        self.t = 0
+        self._in_done = False
+
+    # ---- halo protocol ----------------------------------------------------------------------
+    def exchange_in(self):
+        """Before an odd step: fill the ghost slots the boundary cells will read."""
+        for s in range(len(self.slabs) - 1):
+            lo, up = self.slabs[s], self.slabs[s + 1]
+            top = lo["z1"] - lo["z0"]  # local index of the lower slab's top owned plane
+            up["f"][self.down, 0] = lo["f"][self.down, top]
+            lo["f"][self.up, top + 1] = up["f"][self.up, 1]
+        self._in_done = True
+
+    def exchange_out(self):
+        """After an odd step: return the ghost slots written by fluid boundary cells."""
+        for s in range(len(self.slabs) - 1):
+            lo, up = self.slabs[s], self.slabs[s + 1]
+            top = lo["z1"] - lo["z0"]
+            m_down, m_up = self.masks[s]
+            lo["f"][self.down, top] = torch.where(m_down, up["f"][self.down, 0], lo["f"][self.down, top])
+            up["f"][self.up, 1] = torch.where(m_up, lo["f"][self.up, top + 1], up["f"][self.up, 1])
+        self._in_done = False
+
+    # ---- stepping ------------------------------------------------------------------------
+    def run(self, nsteps: int, reduce: bool = False, want_macro: bool = False):
+        if reduce:
+            self.red.zero_()
+        for i in range(nsteps):
+            odd = self.t & 1
+            if odd and not self._in_done:
+                self.exchange_in()
+            last = i == nsteps - 1
+            for sl in self.slabs:
+                _lib.check(self.lib.pog_step(
+                    sl["p"], _lib.ptr(sl["f"]), _lib.ptr(sl["flags"]), self.t, 1, None, None, None, None, None,
+                    _lib.ptr(sl["rho"]) if (want_macro and last) else None,
+                    _lib.ptr(sl["u"]) if (want_macro and last) else None,
+                    _lib.ptr(self.red) if reduce else None, self._s()))
+            if odd:
+                self.exchange_out()
+            self.t += 1
+        return self.red if reduce else None
+
+    def natural(self, dtype=torch.float64) -> torch.Tensor:
+        """The assembled natural-layout state [19, nz, ny, nx] (exporting an odd-parity state reads
+        the ghost slots, so they are filled first)."""
+        if self.t & 1 and not self._in_done:
+            self.exchange_in()
+        out_store = 3 if dtype == torch.float64 else 0
+        cfg = self.cfg
+        out = torch.empty((19, cfg.nz, cfg.ny, cfg.nx), dtype=dtype, device=self.device)
+        for sl in self.slabs:
+            nat = torch.empty((19,) + tuple(sl["f"].shape[1:]), dtype=dtype, device=self.device)
+            _lib.check(self.lib.pog_export_natural(sl["p"], _lib.ptr(sl["f"]), _lib.ptr(sl["flags"]), self.t,
+                                                   _lib.ptr(nat), out_store, self._s()))
+            out[:, sl["z0"]: sl["z1"]] = nat[:, 1:-1]
+        return out
+
+    def macroscopic(self) -> Tuple[torch.Tensor, torch.Tensor]:
+        """rho [nz, ny, nx] and u [3, nz, ny, nx] written by the last want_macro step."""
+        rho = torch.cat([sl["rho"][1:-1] for sl in self.slabs], dim=0)
+        u = torch.cat([sl["u"][:, 1:-1] for sl in self.slabs], dim=1)
+        return rho, u
+
+
+class RankHalo:
+    """The same halo protocol between processes: this rank holds slab `rank` of `world` as a
+    [19, nz_s + 2, ny, nx] tensor f (its flags as [nz_s + 2, ny, nx]) and trades boundary slots
+    with its neighbours by torch.distributed send/recv (gloo on CPU tensors, NCCL on CUDA)."""
+
+    def __init__(self, flags_slab: np.ndarray, rank: int, world: int):
+        import torch.distributed as dist
+        self.dist = dist
+        self.rank, self.world = rank, world
+        fl = np.asarray(flags_slab)
+        n = fl.shape[0]
+        self.top = n - 2  # local index of the top owned plane
+        # masks for the planes this rank receives back: its top plane's DOWN slots (written by
+        # the upper neighbour's first plane = this rank's top ghost) and its first plane's UP
+        # slots (written by the lower neighbour's top plane = this rank's bottom ghost)
+        self.m_down = torch.as_tensor(writer_masks(fl[n - 1], DOWN))
+        self.m_up = torch.as_tensor(writer_masks(fl[0], UP))
+
+    def _trade(self, send_to, send_buf, recv_from, recv_buf):
+        ops = []
+        if send_to is not None:
+            ops.append(self.dist.P2POp(self.dist.isend, send_buf.contiguous(), send_to))
+        if recv_from is not None:
+            ops.append(self.dist.P2POp(self.dist.irecv, recv_buf, recv_from))
+        if ops:
+            for r in self.dist.batch_isend_irecv(ops):
+                r.wait()
+
+    def exchange_in(self, f: torch.Tensor):
+        below = self.rank - 1 if self.rank > 0 else None
+        above = self.rank + 1 if self.rank < self.world - 1 else None
+        # my top plane's DOWN slots go up into the upper neighbour's bottom ghost
+        buf = torch.empty_like(f[DOWN, 0])
+        self._trade(above, f[DOWN, self.top], below, buf)
+        if below is not None:
+            f[DOWN, 0] = buf
+        # my first plane's UP slots go down into the lower neighbour's top ghost
+        buf = torch.empty_like(f[UP, 0])
+        self._trade(below, f[UP, 1], above, buf)
+        if above is not None:
+            f[UP, self.top + 1] = buf
+
+    def exchange_out(self, f: torch.Tensor):
+        below = self.rank - 1 if self.rank > 0 else None
+        above = self.rank + 1 if self.rank < self.world - 1 else None
+        # my bottom ghost's DOWN slots return to the lower neighbour's top plane
+        buf = torch.empty_like(f[DOWN, 0])
+        self._trade(below, f[DOWN, 0], above, buf)
+        if above is not None:
+            f[DOWN, self.top] = torch.where(self.m_down, buf, f[DOWN, self.top])
+        # my top ghost's UP slots return to the upper neighbour's first plane
+        buf = torch.empty_like(f[UP, 0])
+        self._trade(above, f[UP, self.top + 1], below, buf)
+        if below is not None:
+            f[UP, 1] = torch.where(self.m_up, buf, f[UP, 1])

@@ -1,0 +1,121 @@
+"""z-slab decomposition, CPU: the halo protocol of pour_over_coffee_lbm_gb300.slabs between
+processes (RankHalo over gloo, world size 2 and 3) drives a numpy AA stepper and must reproduce the
+undivided run bit for bit, on a mask whose walls cross the slab interfaces (the masked copy-back
+case) and with flow through them; plus the host-side helpers."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+import np_aa
+from pour_over_coffee_lbm_gb300.slabs import DOWN, UP, RankHalo, slab_bounds, slab_flags, writer_masks
+
+NX, NY, NZ, STEPS, OMEGA = 14, 12, 18, 23, 1.25
+
+
+def _case():
+    rng = np.random.default_rng(5)
+    solid = rng.uniform(size=(NZ, NY, NX)) < 0.12
+    solid[0] = solid[-1] = True
+    solid[:, 0] = solid[:, -1] = True
+    solid[:, :, 0] = solid[:, :, -1] = True
+    flags = np_aa.link_flags(solid)
+    f = np.zeros((19, NZ, NY, NX))
+    fluid = ~solid
+    for q in range(19):
+        f[q][fluid] = np_aa.W[q] * (1.0 + 0.05 * rng.uniform(-1, 1, size=int(fluid.sum())))
+    return flags, f
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, outdir):
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    flags, f = _case()
+    z0, z1 = slab_bounds(NZ, world)[rank]
+    fl = slab_flags(flags, z0, z1)
+    fs = np.zeros((19, z1 - z0 + 2, NY, NX))
+    lo, hi = max(z0 - 1, 0), min(z1 + 1, NZ)
+    fs[:, lo - (z0 - 1): hi - (z0 - 1)] = f[:, lo:hi]
+    ft = torch.from_numpy(fs)  # shares memory with fs
+    halo = RankHalo(fl, rank, world)
+    for t in range(STEPS):
+        if t % 2:
+            halo.exchange_in(ft)
+        np_aa.aa_step(fs, fl, t, OMEGA)
+        if t % 2:
+            halo.exchange_out(ft)
+    if STEPS % 2:
+        halo.exchange_in(ft)  # an odd-parity state is read through the ghost slots
+    np.save(os.path.join(outdir, "slab%d.npy" % rank), fs)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def _natural(f, flags, t):
+    """Natural-layout state of an AA buffer at time t (odd: the odd-step read gather)."""
+    if t % 2 == 0:
+        return f.copy()
+    nz, ny, nx = flags.shape
+    n = nz * ny * nx
+    F = f.reshape(19, n)
+    fl = flags.reshape(n).astype(np.int64)
+    c = np.arange(n)
+    lo = nx * ny + nx + 1
+    live = ((fl & 1) == 0) & (c >= lo) & (c <= n - 1 - lo)
+    out = np.zeros_like(F)
+    cells, flc = c[live], fl[live]
+    off = np_aa.CX + np_aa.CY * nx + np_aa.CZ * nx * ny
+    for q in range(19):
+        wall = (q != 0) & (((flc >> (8 + np_aa.OPP[q])) & 1) == 1)
+        out[q, cells] = np.where(wall, F[q, cells], F[np_aa.OPP[q], cells - off[q]])
+    return out.reshape(f.shape)
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_rank_halo_matches_undivided(tmp_path, world):
+    flags, f = _case()
+    ref = f.copy()
+    for t in range(STEPS):
+        np_aa.aa_step(ref, flags, t, OMEGA)
+    ref_nat = _natural(ref, flags, STEPS)
+    mp.start_processes(_rank, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    got = np.zeros_like(f)
+    for r, (z0, z1) in enumerate(slab_bounds(NZ, world)):
+        fs = np.load(tmp_path / ("slab%d.npy" % r))
+        nat = _natural(fs, slab_flags(flags, z0, z1), STEPS)
+        got[:, z0:z1] = nat[:, 1:-1]
+    live = np.zeros(flags.shape, bool)
+    live[1:-1, 1:-1, 1:-1] = (flags[1:-1, 1:-1, 1:-1] & 1) == 0
+    assert np.array_equal(got[:, live], ref_nat[:, live])
+    assert np.abs(ref_nat[:, live] - f[:, live]).max() > 1e-3  # the state did evolve
+
+
+def test_slab_helpers():
+    assert UP == [5, 11, 12, 15, 16] and DOWN == [6, 13, 14, 17, 18]
+    assert slab_bounds(10, 3) == [(0, 3), (3, 6), (6, 10)]
+    with pytest.raises(ValueError):
+        slab_bounds(4, 3)
+    fl = np.arange(5 * 2 * 2, dtype=np.uint32).reshape(5, 2, 2) * 2  # even: no SOLID bit
+    s = slab_flags(fl, 0, 2)
+    assert (s[0] == 1).all() and np.array_equal(s[1:], fl[:3])
+    s = slab_flags(fl, 3, 5)
+    assert np.array_equal(s[:3], fl[2:5]) and (s[3] == 1).all()
+    plane = np.zeros((4, 5), np.uint32)
+    plane[1, 2] = 1  # one solid writer
+    m = writer_masks(plane, DOWN)
+    for a, q in enumerate(DOWN):
+        cx, cy = int(np_aa.CX[q]), int(np_aa.CY[q])
+        for j in range(4):
+            for i in range(5):
+                jj, ii = j - cy, i - cx
+                inside = 0 <= jj < 4 and 0 <= ii < 5
+                assert m[a, j, i] == (inside and not (jj == 1 and ii == 2))
