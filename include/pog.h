@@ -119,7 +119,44 @@ typedef struct pog_params {
    * overrides u_inlet/inlet_coef when non-null, so a time-varying pour is fed by one small
    * host-to-device copy per step (and survives CUDA-graph replay).  NULL = use the fields. */
   const float* inlet_control;
+  /* Optional DEVICE pointer to a pour-nozzle block (POG_POUR_* below) or NULL.  While its
+   * ACTIVE field is non-zero, pog_step adds the nozzle's downward force to the fluid and
+   * pog_particles_couple adds the stream's impact force to the particles near it. */
+  const float* pour_control;
 } pog_params;
+
+/* Pour-nozzle block, floats (PrecisePouringSystem, src/physics/precise_pouring.py:12-193):
+ * a stream of radius R ending at plane ZTOP, HEIGHT planes tall, centred at (X, Y).  A fluid cell
+ * at distance r <= R from the axis on plane ZTOP - HEIGHT <= k <= ZTOP receives the force
+ * density -min(VELOCITY * I * FLOW / DT, ACCEL_CAP) e_z, I = exp(-(r/R)^2 / 2) exp(-(ZTOP - k)/2)
+ * (apply_pouring_force :132-160, _is_in_pouring_region :100-130).  pog_pour_advance moves the
+ * nozzle: TIME += DT, then (X, Y) = (CX, CY) (PATTERN 0) or the growing spiral (PATTERN 1)
+ * t = TIME*SPIRAL_SPEED, r = SPIRAL_R (1 + 0.1 t), (CX + r cos t, CY + r sin t) clamped to
+ * [DIAMETER, nx - DIAMETER] x [DIAMETER, ny - DIAMETER] (_get_current_pour_position :81-98).
+ * A particle within 2R of the axis and above IMPACT_ZMIN feels -IMPACT I e_z plus a radial push
+ * 0.3 IMPACT I along (dx, dy)/r (for r > 0.1), I = exp(-(r/R)^2 / 2), |F| <= IMPACT_MAX
+ * (create_water_impact_force :190-226); IMPACT = 0 turns it off. */
+#define POG_POUR_ACTIVE 0
+#define POG_POUR_X 1
+#define POG_POUR_Y 2
+#define POG_POUR_RADIUS 3
+#define POG_POUR_ZTOP 4
+#define POG_POUR_HEIGHT 5
+#define POG_POUR_VELOCITY 6
+#define POG_POUR_FLOW 7
+#define POG_POUR_DT 8
+#define POG_POUR_ACCEL_CAP 9
+#define POG_POUR_PATTERN 10
+#define POG_POUR_CX 11
+#define POG_POUR_CY 12
+#define POG_POUR_SPIRAL_R 13
+#define POG_POUR_SPIRAL_SPEED 14
+#define POG_POUR_TIME 15
+#define POG_POUR_DIAMETER 16
+#define POG_POUR_IMPACT 17
+#define POG_POUR_IMPACT_MAX 18
+#define POG_POUR_IMPACT_ZMIN 19
+#define POG_POUR_NFIELDS 20
 
 /* Reduction slots written by pog_step when `reductions` is non-null (FP64, accumulated with
  * atomics: zero them before a call to get that call's sums).  Replaces the host-side np.sum
@@ -153,6 +190,11 @@ long long pog_launch_count(int reset);
 
 /* Check a parameter block (sizes, enum values, ranges).  Host only. */
 int pog_validate_params(const pog_params* p);
+
+/* Advance the pour nozzle of p->pour_control by one step on the device (TIME += DT and the new
+ * (X, Y), see above), so a captured CUDA graph replays a moving nozzle.  No-op while ACTIVE is 0.
+ * POG_E_ARG without a pour block. */
+int pog_pour_advance(const pog_params* p, void* stream);
 
 /* ---- geometry ------------------------------------------------------------------------------ */
 /* Build the cell flag words (own flags + the 18 solid-neighbour link bits) of the V60 mask,

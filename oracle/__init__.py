@@ -49,13 +49,26 @@ def load():
             lib.orc_round_storage.restype = ctypes.c_float
             lib.orc_round_storage.argtypes = [_i, ctypes.c_float, _i, ctypes.c_float]
             lib.orc_inlet_velocity_f64.argtypes = [_v, _v, _v, _i]
+            lib.orc_pour_advance.restype = None
+            lib.orc_pour_advance.argtypes = [_v, _v]
             _lib = lib
         return _lib
 
 
-def _params(cfg):
+def _params(cfg, pour=None):
+    """ctypes params of cfg; `pour` (float32 [POG_POUR_NFIELDS] host array) becomes the
+    restatement's pour-nozzle block."""
     p = cfg.to_c()
+    if pour is not None:
+        p.pour_control = pour.ctypes.data_as(ctypes.c_void_p).value
     return p, ctypes.byref(p)
+
+
+def pour_advance(cfg, pour):
+    """One nozzle step of a host pour block, in place."""
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_pour_advance(pp, _p(pour))
 
 
 def tables():
@@ -86,11 +99,11 @@ def init_equilibrium(cfg, flags, dtype=np.float64, rho0=None, u0=(0.0, 0.0, 0.0)
     return f
 
 
-def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdrag=None):
+def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdrag=None, pour=None):
     """One push step.  force: [3][n] explicit force; pdrag: [4][n] particle drag deposit
-    (Kp, Kv).  Returns (f_next, rho, u)."""
+    (Kp, Kv); pour: host pour-nozzle block.  Returns (f_next, rho, u)."""
     lib = load()
-    _, pp = _params(cfg)
+    _keep, pp = _params(cfg, pour)
     dt = f.dtype
     fo = f.copy()
     rho = np.zeros((cfg.nz, cfg.ny, cfg.nx), dt)
@@ -192,12 +205,12 @@ def particles_bin(cfg, pos, active):
     return keys, perm
 
 
-def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=None):
+def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=None, pour=None):
     """One coupling pass (serial, id order) on copies of the state.  Returns the updated
     (pos, vel, drag_old, active, force_fix, u_at); force_fix is the [4][n] int64 drag deposit
-    (Kp, Kv) scaled by 2^32."""
+    (Kp, Kv) scaled by 2^32.  pour: host pour-nozzle block (impact force)."""
     lib = load()
-    _, pp = _params(cfg)
+    _keep, pp = _params(cfg, pour)
     ppp = pcfg.to_c()
     pos = np.ascontiguousarray(pos, np.float32).copy()
     vel = np.ascontiguousarray(vel, np.float32).copy()

@@ -188,6 +188,25 @@ T les_nu_stencil(const pog_params* p, const Geo& g, const uint32_t* flags, const
 // forcing, filter_paper.py:471-536 porous drag, boundary_conditions.py:384-409 inlet/outlet).
 // Inputs: incoming populations f, flag, optional external force Fe and porosity.  Output:
 // post-collision populations fs, rho, u, and reduction contributions.
+// Pour nozzle (precise_pouring.py:100-160).  For the restatement `pour_control` is a HOST copy of
+// the POG_POUR_* block: the stream cylinder's downward force density on cell (i, j, k).
+template <typename T>
+T pour_accel(const float* b, int nz, int i, int j, int k) {
+  if (b[POG_POUR_ACTIVE] == 0.0f) return (T)0;
+  const float ztop = b[POG_POUR_ZTOP];
+  if (!((float)k <= ztop && (float)k >= ztop - b[POG_POUR_HEIGHT]) || k < 0 || k > nz - 1) return (T)0;
+  const T dx = (T)i - (T)b[POG_POUR_X], dy = (T)j - (T)b[POG_POUR_Y];
+  const T R = (T)b[POG_POUR_RADIUS];
+  const T d = sqrt(dx * dx + dy * dy);
+  if (!(d <= R)) return (T)0;
+  const T dr = d / R;
+  const T I = exp((T)-0.5 * dr * dr) * exp(-((T)ztop - (T)k) / (T)2);
+  const T dt = (T)b[POG_POUR_DT];
+  T a = dt > (T)1e-8 ? (T)b[POG_POUR_VELOCITY] * I * (T)b[POG_POUR_FLOW] / dt : (T)0;
+  const T cap = (T)b[POG_POUR_ACCEL_CAP];
+  return a < cap ? a : cap;
+}
+
 template <typename T>
 void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int k, const T f[19],
              const T* Fe, const T* Pd, bool has_eps, T eps, T nu_stencil, T fs[19], T& rho_o,
@@ -221,6 +240,7 @@ void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int
       Gy += Fe[1];
       Gz += Fe[2];
     }
+    if (p->pour_control) Gz -= pour_accel<T>(p->pour_control, p->nz, i, j, k);
     // particle drag deposit Pd = (Kp, Kv): fluid force Kv - Kp u, implicit in u
     T Kp = 0, Kvx = 0, Kvy = 0, Kvz = 0;
     if (Pd) {
@@ -593,6 +613,22 @@ int orc_porous_force_f32(const pog_params* p, const uint32_t* flags, const float
 void orc_inlet_velocity_f64(const pog_params* p, const double* r, double* uz, int m) {
   for (int i = 0; i < m; ++i) uz[i] = inlet_velocity<double>(p, r[i]);
 }
+// One nozzle step of a host pour block (pour_advance_kernel in the library).
+void orc_pour_advance(const pog_params* p, float* b) {
+  if (b[POG_POUR_ACTIVE] == 0.0f) return;
+  const float time = b[POG_POUR_TIME] + b[POG_POUR_DT];
+  b[POG_POUR_TIME] = time;
+  float x = b[POG_POUR_CX], y = b[POG_POUR_CY];
+  if (b[POG_POUR_PATTERN] == 1.0f) {
+    const float t = time * b[POG_POUR_SPIRAL_SPEED];
+    const float r = b[POG_POUR_SPIRAL_R] * (1.0f + 0.1f * t);
+    const float d = b[POG_POUR_DIAMETER];
+    x = std::fmax(d, std::fmin((float)p->nx - d, x + r * std::cos(t)));
+    y = std::fmax(d, std::fmin((float)p->ny - d, y + r * std::sin(t)));
+  }
+  b[POG_POUR_X] = x;
+  b[POG_POUR_Y] = y;
+}
 float orc_round_storage(int storage, float v, int q, float rho0) {
   return store_round<float>(storage, v, q, rho0);
 }
@@ -647,6 +683,11 @@ inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
 inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
 inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
 inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+inline Dual exp(const Dual& a) {
+  Dual r(::exp(a.v));
+  for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * r.v;
+  return r;
+}
 inline Dual sqrt(const Dual& a) {
   Dual r(::sqrt(a.v));
   double g = a.v > 0 ? 0.5 / r.v : 0.0;  // zero subgradient at 0, as the CUDA adjoint

@@ -185,8 +185,34 @@ int orc_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
       drag_old[a * np + q] = F[a];
     }
     float nv[3], np3[3] = {x, y, z};
+    // impact of the pour stream (create_water_impact_force, precise_pouring.py:190-226)
+    float Fi[3] = {0.0f, 0.0f, 0.0f};
+    bool impact = false;
+    const float* b = p->pour_control;  // host copy of the POG_POUR_* block
+    if (b && b[POG_POUR_ACTIVE] != 0.0f && b[POG_POUR_IMPACT] > 0.0f) {
+      const float dx = x - b[POG_POUR_X], dy = y - b[POG_POUR_Y];
+      const float R = b[POG_POUR_RADIUS];
+      const float r = sqrtf(dx * dx + dy * dy);
+      if (r <= R * 2.0f && z > b[POG_POUR_IMPACT_ZMIN]) {
+        impact = true;
+        const float S = b[POG_POUR_IMPACT];
+        const float rr = r / R;
+        const float I = expf(-0.5f * (rr * rr));
+        Fi[2] = -S * I;
+        if (r > 0.1f) {
+          const float rm = S * 0.3f * I;
+          Fi[0] = rm * dx / r;
+          Fi[1] = rm * dy / r;
+        }
+        const float fm = sqrtf(Fi[0] * Fi[0] + Fi[1] * Fi[1] + Fi[2] * Fi[2]);
+        if (fm > b[POG_POUR_IMPACT_MAX]) {
+          const float sc = b[POG_POUR_IMPACT_MAX] / fm;
+          for (int a = 0; a < 3; ++a) Fi[a] = Fi[a] * sc;
+        }
+      }
+    }
     for (int a = 0; a < 3; ++a) {
-      float acc = (F[a] + (mp - mf) * gvec[a]) / mp;
+      float acc = impact ? (F[a] + (mp - mf) * gvec[a] + Fi[a]) / mp : (F[a] + (mp - mf) * gvec[a]) / mp;
       nv[a] = v0[a] + acc * dt;
       np3[a] = np3[a] + nv[a] * dt;
     }

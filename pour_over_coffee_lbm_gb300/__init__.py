@@ -19,6 +19,7 @@ __all__ = [
     "LatticeConfig", "ParticleConfig", "GB300LBMSolver", "UnifiedLBMSolver",
     "create_unified_solver", "CoffeeParticleSystem", "OutflowAdjoint", "outflow_loss",
     "LBMSolverProtocol", "ParticleCoupledLBMProtocol", "validate_lbm_solver",
+    "PrecisePouringSystem", "SlabLattice",
 ]
 
 
@@ -34,4 +35,10 @@ def __getattr__(name):
     if name in ("OutflowAdjoint", "outflow_loss", "OutflowLoss"):
         from . import adjoint
         return getattr(adjoint, name)
+    if name == "PrecisePouringSystem":
+        from .pouring import PrecisePouringSystem
+        return PrecisePouringSystem
+    if name == "SlabLattice":
+        from .slabs import SlabLattice
+        return SlabLattice
     raise AttributeError(name)

@@ -26,6 +26,7 @@ SOURCES = {
     "particles.cu": ["-fmad=false"],
     "particles_noalloc.cu": [],
     "adjoint.cu": [],
+    "pour.cu": [],
 }
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -58,6 +58,34 @@ __host__ __device__ __forceinline__ C feq_q(int q, C rho, C ux, C uy, C uz, C us
   return (C)wd(q) * rho * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - usq15);
 }
 
+// Downward force density of the pour nozzle on cell c (POG_POUR_* block, precise_pouring.py:
+// 100-160): 0 outside the stream cylinder, else min(velocity I flow / dt, cap) with the Gaussian
+// radial and exponential vertical intensity I.  Cells outside the stream's planes leave after one
+// index compare, so the term costs a full cell only inside the nozzle.  Out of line: its
+// registers are not reserved in the step kernel's main path.
+template <typename C>
+__device__ __noinline__ C pour_accel(const KParams& kp, uint32_t c) {
+  const float* b = kp.pour;
+  if (b[POG_POUR_ACTIVE] == 0.0f) return (C)0;
+  const float ztop = b[POG_POUR_ZTOP];
+  const float klo = ceilf(ztop - b[POG_POUR_HEIGHT]), khi = floorf(ztop);
+  if (!(khi >= 0.0f) || klo > (float)(kp.nz - 1) || khi < klo) return (C)0;
+  const uint32_t c0 = (uint32_t)fmaxf(klo, 0.0f) * kp.nxny;
+  const uint32_t c1 = ((uint32_t)fminf(khi, (float)(kp.nz - 1)) + 1u) * kp.nxny;
+  if (c < c0 || c >= c1) return (C)0;
+  const uint32_t k = c / kp.nxny, rem = c - k * kp.nxny, j = rem / kp.nx, i = rem - j * kp.nx;
+  const C dx = (C)i - (C)b[POG_POUR_X], dy = (C)j - (C)b[POG_POUR_Y];
+  const C R = (C)b[POG_POUR_RADIUS];
+  const C d = sqrt(dx * dx + dy * dy);
+  if (!(d <= R)) return (C)0;
+  const C dr = d / R;
+  const C I = exp((C)-0.5 * dr * dr) * exp(-((C)ztop - (C)k) / (C)2);
+  const C dt = (C)b[POG_POUR_DT];
+  C a = dt > (C)1e-8 ? (C)b[POG_POUR_VELOCITY] * I * (C)b[POG_POUR_FLOW] / dt : (C)0;
+  const C cap = (C)b[POG_POUR_ACCEL_CAP];
+  return a < cap ? a : cap;
+}
+
 // f_eq_q - w_q rs for a density rr = rs + dr, without forming f_eq_q: w_q (dr + rr (3 e.u +
 // 4.5 (e.u)^2 - 1.5 u.u)).
 template <typename C>
@@ -188,6 +216,7 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     Gy += (C)force[kp.n + c];
     Gz += (C)force[2u * kp.n + c];
   }
+  if (kp.pour) Gz -= pour_accel<C>(kp, c);
   const C inv_rho = (C)1 / rho;
   // Particle drag deposit: F_p = Kv - Kp u with u implicit.  v is the velocity with every
   // explicit force, A the implicit factor (1 without particles).

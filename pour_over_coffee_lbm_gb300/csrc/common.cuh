@@ -61,6 +61,7 @@ struct KParams {
   float u_inlet, inlet_R, cxf, cyf, rho_out;
   float coef[POG_INLET_NCOEF];
   const float* inlet_ctl;  // device [u_inlet, a_0..a_15] or null
+  const float* pour;       // device pour-nozzle block (POG_POUR_*) or null
 };
 
 KParams make_kparams(const pog_params* p);

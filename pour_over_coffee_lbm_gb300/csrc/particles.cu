@@ -186,7 +186,39 @@ struct PKParams {
   float rho0, mu, rho_p, alpha, dt, gx, gy, gz;
   float zlo, zhi, margin, pullback, damping;
   int drag_model, deterministic;
+  const float* pour;  // device pour-nozzle block or null
 };
+
+// Impact force of the pour stream on a particle at (x, y, z) (create_water_impact_force,
+// precise_pouring.py:190-226): within 2R of the stream axis and above IMPACT_ZMIN, -S I e_z
+// plus the radial push 0.3 S I (dx, dy)/r, I = exp(-(r/R)^2 / 2), |F| capped at IMPACT_MAX.
+__device__ __forceinline__ bool pour_impact(const float* b, float x, float y, float z, float Fi[3]) {
+  if (b[POG_POUR_ACTIVE] == 0.0f || !(b[POG_POUR_IMPACT] > 0.0f)) return false;
+  const float dx = x - b[POG_POUR_X], dy = y - b[POG_POUR_Y];
+  const float R = b[POG_POUR_RADIUS];
+  const float r = sqrtf(dx * dx + dy * dy);
+  if (!(r <= R * 2.0f) || !(z > b[POG_POUR_IMPACT_ZMIN])) return false;
+  const float S = b[POG_POUR_IMPACT];
+  const float rr = r / R;
+  const float I = expf(-0.5f * (rr * rr));
+  Fi[0] = 0.0f;
+  Fi[1] = 0.0f;
+  Fi[2] = -S * I;
+  if (r > 0.1f) {
+    const float rm = S * 0.3f * I;
+    Fi[0] = rm * dx / r;
+    Fi[1] = rm * dy / r;
+  }
+  const float fm = sqrtf(Fi[0] * Fi[0] + Fi[1] * Fi[1] + Fi[2] * Fi[2]);
+  const float mx = b[POG_POUR_IMPACT_MAX];
+  if (fm > mx) {
+    const float sc = mx / fm;
+    Fi[0] = Fi[0] * sc;
+    Fi[1] = Fi[1] * sc;
+    Fi[2] = Fi[2] * sc;
+  }
+  return true;
+}
 
 // Segmented warp sum over runs of consecutive lanes that share `node` (in cell order equal
 // nodes are consecutive; in any other order a repeated node simply starts a new run).  Runs
@@ -293,9 +325,11 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
         drag_old[a * np + q] = F[a];
       }
       float nv[3], np3[3] = {x, y, z};
+      float Fi[3];
+      const bool impact = P.pour && pour_impact(P.pour, x, y, z, Fi);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
-        float acc = (F[a] + (mp - mf) * gv[a]) / mp;
+        float acc = impact ? (F[a] + (mp - mf) * gv[a] + Fi[a]) / mp : (F[a] + (mp - mf) * gv[a]) / mp;
         nv[a] = v0[a] + acc * P.dt;
         np3[a] = np3[a] + nv[a] * P.dt;
       }
@@ -485,6 +519,7 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   P.damping = pp->wall_damping;
   P.drag_model = pp->drag_model;
   P.deterministic = pp->deterministic;
+  P.pour = p->pour_control;
   cudaStream_t s = (cudaStream_t)stream;
   int block = 256;
   int grid = (np + block - 1) / block;

@@ -42,6 +42,7 @@ class PogParams(ctypes.Structure):
         ("u_inlet", ctypes.c_float), ("inlet_coef", ctypes.c_float * INLET_NCOEF),
         ("rho_outlet", ctypes.c_float),
         ("inlet_control", ctypes.c_void_p),
+        ("pour_control", ctypes.c_void_p),
     ]
 
 

@@ -162,6 +162,7 @@ class GB300LBMSolver:
         self._red = torch.zeros(RED_COUNT, dtype=torch.float64, device=dev)
         self._porosity = None
         self._inlet_ctl = None
+        self._pour_ctl = None
         if porosity is not None:
             self.set_porosity(porosity)
         self.t = 0
@@ -426,6 +427,16 @@ class GB300LBMSolver:
             control = control.contiguous()
         self._inlet_ctl = control
         self._p.inlet_control = None if control is None else control.data_ptr()
+
+    def set_pour_control(self, block: Optional[torch.Tensor]) -> None:
+        """Attach a pour-nozzle block (PrecisePouringSystem.block: CUDA float32, POG_POUR_NFIELDS
+        values) read by the step kernel and the particle coupling; None detaches it."""
+        if block is not None:
+            if block.dtype != torch.float32 or block.numel() != 20 or not block.is_cuda or not block.is_contiguous():
+                raise ValueError("pour block must be a contiguous CUDA float32 tensor of 20 values")
+        self._pour_ctl = block
+        self._p.pour_control = None if block is None else block.data_ptr()
+        self._macro_dirty = True
 
     def capture(self, nsteps: int, particle_system=None, dt: float = 1.0,
                 relaxation_factor: float = 0.8) -> "StepGraph":
