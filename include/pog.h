@@ -196,6 +196,33 @@ int pog_validate_params(const pog_params* p);
  * POG_E_ARG without a pour block. */
 int pog_pour_advance(const pog_params* p, void* stream);
 
+/* ---- diagnostics ----------------------------------------------------------------------------- */
+/* Field statistics of rho [ncell] and u [3][ncell] (FP32, every cell of the grid, as the
+ * reference's host-side LBMDiagnostics computes them from to_numpy() copies,
+ * src/visualization/lbm_diagnostics.py:151-460), in one device pass.  stats receives
+ * POG_STAT_COUNT doubles (zeroed by the call); rho_prev/u_prev (nullable) feed the temporal
+ * change sums; zprofile (nullable) receives the nz per-plane sums of rho.  |u| thresholds are in
+ * lattice units: 1e-10 (active cells) and 0.1 c_s (Mach 0.1).  Region sums split the planes at
+ * int(0.3 nz) and int(0.8 nz) (detailed_flow_analysis :393-402). */
+#define POG_STAT_MASS 0        /* sum rho                                                     */
+#define POG_STAT_RHO2 1        /* sum rho^2                                                   */
+#define POG_STAT_MOMX 2        /* sum rho u_x (3 slots: x, y, z)                               */
+#define POG_STAT_UMAX 5        /* max |u|                                                     */
+#define POG_STAT_UACT_SUM 6    /* sum |u| over |u| > 1e-10                                    */
+#define POG_STAT_UACT_N 7      /* number of cells with |u| > 1e-10                            */
+#define POG_STAT_U2 8          /* sum |u|^2                                                   */
+#define POG_STAT_UABS 9        /* sum |u|                                                     */
+#define POG_STAT_MACH_N 10     /* number of cells with |u| > 0.1 c_s                          */
+#define POG_STAT_DRHO_MAX 11   /* max |rho - rho0|                                            */
+#define POG_STAT_DRHO2 12      /* sum (rho - rho_prev)^2                                      */
+#define POG_STAT_DU2 13        /* sum |u - u_prev|^2                                          */
+#define POG_STAT_USUM 14       /* sum u_a (3 slots)                                           */
+#define POG_STAT_USQ 17        /* sum u_a^2 (3 slots)                                         */
+#define POG_STAT_UREG 20       /* sum |u| over planes [0,z30), [z30,z80), [z80,nz) (3 slots)  */
+#define POG_STAT_COUNT 23
+int pog_field_stats(const pog_params* p, const float* rho, const float* u, const float* rho_prev,
+                    const float* u_prev, double* stats, double* zprofile, void* stream);
+
 /* ---- geometry ------------------------------------------------------------------------------ */
 /* Build the cell flag words (own flags + the 18 solid-neighbour link bits) of the V60 mask,
  * drain hole, inlet/outlet disks and porous band: flags[c], c = (k*ny + j)*nx + i.

@@ -19,7 +19,7 @@ __all__ = [
     "LatticeConfig", "ParticleConfig", "GB300LBMSolver", "UnifiedLBMSolver",
     "create_unified_solver", "CoffeeParticleSystem", "OutflowAdjoint", "outflow_loss",
     "LBMSolverProtocol", "ParticleCoupledLBMProtocol", "validate_lbm_solver",
-    "PrecisePouringSystem", "SlabLattice",
+    "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter",
 ]
 
 
@@ -38,6 +38,9 @@ def __getattr__(name):
     if name == "PrecisePouringSystem":
         from .pouring import PrecisePouringSystem
         return PrecisePouringSystem
+    if name in ("LBMDiagnostics", "SnapshotWriter"):
+        from . import diagnostics
+        return getattr(diagnostics, name)
     if name == "SlabLattice":
         from .slabs import SlabLattice
         return SlabLattice

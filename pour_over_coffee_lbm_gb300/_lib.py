@@ -31,6 +31,7 @@ SIGNATURES = [
     ("pog_build_flags", _i, [_P, _v, _v]),
     ("pog_init_equilibrium", _i, [_P, _v, _v, _f, _f, _f, _f, _v]),
     ("pog_pour_advance", _i, [_P, _v]),
+    ("pog_field_stats", _i, [_P, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_step", _i, [_P, _v, _v, _ll, _i, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_step_push", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_export_natural", _i, [_P, _v, _v, _ll, _v, _i, _v]),

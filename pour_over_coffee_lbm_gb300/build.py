@@ -27,6 +27,7 @@ SOURCES = {
     "particles_noalloc.cu": [],
     "adjoint.cu": [],
     "pour.cu": [],
+    "diag.cu": [],
 }
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -428,6 +428,16 @@ class GB300LBMSolver:
         self._inlet_ctl = control
         self._p.inlet_control = None if control is None else control.data_ptr()
 
+    def save_checkpoint(self, path: str, particles=None, pour=None) -> None:
+        """Raw state of the run (and of its particles / pour nozzle) to an .npz file that
+        load_checkpoint continues bit for bit."""
+        from .diagnostics import save_checkpoint
+        save_checkpoint(path, self, particles, pour)
+
+    def load_checkpoint(self, path: str, particles=None, pour=None) -> None:
+        from .diagnostics import load_checkpoint
+        load_checkpoint(path, self, particles, pour)
+
     def set_pour_control(self, block: Optional[torch.Tensor]) -> None:
         """Attach a pour-nozzle block (PrecisePouringSystem.block: CUDA float32, POG_POUR_NFIELDS
         values) read by the step kernel and the particle coupling; None detaches it."""
