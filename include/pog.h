@@ -123,6 +123,10 @@ typedef struct pog_params {
    * ACTIVE field is non-zero, pog_step adds the nozzle's downward force to the fluid and
    * pog_particles_couple adds the stream's impact force to the particles near it. */
   const float* pour_control;
+  /* Optional DEVICE pointer to the filter-paper blockage field b [ncell] (pog_filter_update) or
+   * NULL: porous cells scale their Darcy and Forchheimer coefficients by (1 + b[c])
+   * (apply_filter_effects' blockage_factor, filter_paper.py:584-587). */
+  const float* filter_blockage;
 } pog_params;
 
 /* Pour-nozzle block, floats (PrecisePouringSystem, src/physics/precise_pouring.py:12-193):
@@ -195,6 +199,21 @@ int pog_validate_params(const pog_params* p);
  * (X, Y), see above), so a captured CUDA graph replays a moving nozzle.  No-op while ACTIVE is 0.
  * POG_E_ARG without a pour block. */
 int pog_pour_advance(const pog_params* p, void* stream);
+
+/* ---- filter-paper dynamics (FilterPaperSystem.step, filter_paper.py:616-790) ------------------ */
+/* Particles meeting the paper: each active particle at cell (i, j, k) = int(pos) looks for a
+ * porous cell at (i, j, k + o), o = -2..2 in that order; at the first one, a particle moving
+ * down (v_z < 0) bounces with v_z := -0.3 v_z, gets a horizontal roughness kick of +-0.005 per
+ * axis, and adds 0.01 to accum at that cell (block_particles_at_filter, :616-700).  The kicks
+ * come from a counter-based hash of (seed, step, particle): lowbias32 (C. Wellons), so runs
+ * are reproducible.  accum [ncell] is added to atomically. */
+int pog_filter_particles(const pog_params* p, const uint32_t* flags, const float* pos, float* vel,
+                         const int32_t* active, int np, float* accum, uint32_t seed, long long step,
+                         void* stream);
+/* Dynamic blockage of the porous cells (update_dynamic_resistance, :702-750):
+ * b := 0.95 b + 0.05 * 0.9 (1 - exp(-0.1 accum)), accum := 0.999 accum. */
+int pog_filter_update(const pog_params* p, const uint32_t* flags, float* accum, float* blockage,
+                      void* stream);
 
 /* ---- diagnostics ----------------------------------------------------------------------------- */
 /* Field statistics of rho [ncell] and u [3][ncell] (FP32, every cell of the grid, as the
@@ -338,7 +357,8 @@ int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* 
  *   The loss is J = sum_t flux_t with flux_t = POG_RED_OUTFLOW of step t, so each outlet
  *   cell adds dJ/df_i = -c_iz.  Parameter gradients are accumulated in FP64:
  *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
- *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL. */
+ *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL,
+ *   pour_control and filter_blockage NULL (POG_E_ARG otherwise). */
 int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next, void* lam_t,
                      const uint32_t* flags, const float* porosity, double* grad_porosity,
                      double* grad_inlet, void* stream);

@@ -50,6 +50,8 @@ def load():
             lib.orc_round_storage.argtypes = [_i, ctypes.c_float, _i, ctypes.c_float]
             lib.orc_inlet_velocity_f64.argtypes = [_v, _v, _v, _i]
             lib.orc_pour_advance.restype = None
+            lib.orc_filter_particles.restype = None
+            lib.orc_filter_update.restype = None
             lib.orc_pour_advance.argtypes = [_v, _v]
             _lib = lib
         return _lib
@@ -62,6 +64,26 @@ def _params(cfg, pour=None):
     if pour is not None:
         p.pour_control = pour.ctypes.data_as(ctypes.c_void_p).value
     return p, ctypes.byref(p)
+
+
+def filter_particles(cfg, flags, pos, vel, active, accum, seed, step):
+    """Particle-filter bounce (in place on vel and accum).  flags uint32 [ncell], pos/vel float32
+    [3][np], active int32 [np], accum float32 [ncell], all C-contiguous."""
+    for a, dt in ((flags, np.uint32), (pos, np.float32), (vel, np.float32), (active, np.int32), (accum, np.float32)):
+        assert a.dtype == dt and a.flags.c_contiguous
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_filter_particles(pp, _p(flags), _p(pos), _p(vel), _p(active), int(active.shape[0]), _p(accum),
+                             ctypes.c_uint32(seed), ctypes.c_longlong(step))
+
+
+def filter_update(cfg, flags, accum, blockage):
+    """Blockage update of the porous cells (in place on accum and blockage, float32 [ncell])."""
+    for a, dt in ((flags, np.uint32), (accum, np.float32), (blockage, np.float32)):
+        assert a.dtype == dt and a.flags.c_contiguous
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_filter_update(pp, _p(flags), _p(accum), _p(blockage))
 
 
 def pour_advance(cfg, pour):
@@ -99,11 +121,16 @@ def init_equilibrium(cfg, flags, dtype=np.float64, rho0=None, u0=(0.0, 0.0, 0.0)
     return f
 
 
-def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdrag=None, pour=None):
+def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdrag=None, pour=None,
+         blockage=None):
     """One push step.  force: [3][n] explicit force; pdrag: [4][n] particle drag deposit
-    (Kp, Kv); pour: host pour-nozzle block.  Returns (f_next, rho, u)."""
+    (Kp, Kv); pour: host pour-nozzle block; blockage: [n] filter blockage.  Returns
+    (f_next, rho, u)."""
     lib = load()
     _keep, pp = _params(cfg, pour)
+    if blockage is not None:
+        blockage = np.ascontiguousarray(blockage, np.float32)
+        _keep.filter_blockage = blockage.ctypes.data_as(ctypes.c_void_p).value
     dt = f.dtype
     fo = f.copy()
     rho = np.zeros((cfg.nz, cfg.ny, cfg.nx), dt)

@@ -267,24 +267,28 @@ void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int
         CF = (T)p->forchheimer;
       }
       T sK = sqrt(K);
+      // Darcy and Forchheimer coefficients times the filter blockage factor 1 + b (for the
+      // restatement `filter_blockage` is a HOST array)
+      const T bf = p->filter_blockage ? (T)1 + (T)p->filter_blockage[g.idx(i, j, k)] : (T)1;
+      const T dk = nu0 / K * bf, fk = CF / sK * bf;
       if (p->drag_mode == POG_DRAG_SEMI_IMPLICIT) {
         // u (A + nu/(2K) + C_F |u| / (2 sqrt K)) = v
-        T c0 = (T)0.5 * (A + (T)0.5 * nu0 / K);
-        T c1 = (T)0.5 * CF / sK;
+        T c0 = (T)0.5 * (A + (T)0.5 * dk);
+        T c1 = (T)0.5 * fk;
         T vm = sqrt(vx * vx + vy * vy + vz * vz);
         T s = (T)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
         ux = vx * s;
         uy = vy * s;
         uz = vz * s;
         T um = sqrt(ux * ux + uy * uy + uz * uz);
-        T coef = rho * (nu0 / K + CF / sK * um);
+        T coef = rho * (dk + fk * um);
         Fx = Gx + Kvx - (coef + Kp) * ux;
         Fy = Gy + Kvy - (coef + Kp) * uy;
         Fz = Gz + Kvz - (coef + Kp) * uz;
       } else {
         T wx = vx / A, wy = vy / A, wz = vz / A;  // velocity before the porous drag
         T vm = sqrt(wx * wx + wy * wy + wz * wz);
-        T coef = rho * (nu0 / K + CF / sK * vm);
+        T coef = rho * (dk + fk * vm);
         T dx = -coef * wx, dy = -coef * wy, dz = -coef * wz;
         T dm = sqrt(dx * dx + dy * dy + dz * dz);
         T cap = (T)p->drag_cap;
@@ -613,6 +617,56 @@ int orc_porous_force_f32(const pog_params* p, const uint32_t* flags, const float
 void orc_inlet_velocity_f64(const pog_params* p, const double* r, double* uz, int m) {
   for (int i = 0; i < m; ++i) uz[i] = inlet_velocity<double>(p, r[i]);
 }
+// Filter-paper dynamics (filter_paper.py:616-750), the library's filter.cu restated: the
+// particle bounce with the lowbias32 roughness kicks, and the blockage update.
+static uint32_t lowbias32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+static float hash_uniform(uint32_t seed, uint32_t step, uint32_t id, uint32_t lane) {
+  const uint32_t h = lowbias32(seed ^ lowbias32(step ^ lowbias32(id * 2u + lane)));
+  return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+void orc_filter_particles(const pog_params* p, const uint32_t* flags, const float* pos, float* vel,
+                          const int32_t* active, int np, float* accum, uint32_t seed, long long step) {
+  const uint32_t nx = p->nx, ny = p->ny, nz = p->nz;
+  for (int q = 0; q < np; ++q) {
+    if (!active[q]) continue;
+    const float x = pos[q], y = pos[np + q], z = pos[2 * np + q];
+    if (!(x >= 0.0f && y >= 0.0f && z >= 0.0f)) continue;
+    const uint32_t i = (uint32_t)x, j = (uint32_t)y, k = (uint32_t)z;
+    if (i >= nx || j >= ny || k >= nz) continue;
+    for (int o = -2; o <= 2; ++o) {
+      const int kk = (int)k + o;
+      if (kk < 0 || kk >= (int)nz) continue;
+      const uint32_t c = ((uint32_t)kk * ny + j) * nx + i;
+      if (!(flags[c] & POG_CELL_POROUS)) continue;
+      const float vz = vel[2 * np + q];
+      if (vz < 0.0f) {
+        vel[2 * np + q] = -vz * 0.3f;
+        vel[q] = vel[q] + (hash_uniform(seed, (uint32_t)step, (uint32_t)q, 0u) - 0.5f) * 0.01f;
+        vel[np + q] = vel[np + q] + (hash_uniform(seed, (uint32_t)step, (uint32_t)q, 1u) - 0.5f) * 0.01f;
+        accum[c] = accum[c] + 0.01f;
+      }
+      break;
+    }
+  }
+}
+void orc_filter_update(const pog_params* p, const uint32_t* flags, float* accum, float* blockage) {
+  const long long n = (long long)p->nx * p->ny * p->nz;
+  for (long long c = 0; c < n; ++c) {
+    if (!(flags[c] & POG_CELL_POROUS)) continue;
+    const float a = accum[c];
+    const float nb = 0.9f * (1.0f - expf(-0.1f * a));
+    blockage[c] = 0.95f * blockage[c] + 0.05f * nb;
+    accum[c] = a * 0.999f;
+  }
+}
+
 // One nozzle step of a host pour block (pour_advance_kernel in the library).
 void orc_pour_advance(const pog_params* p, float* b) {
   if (b[POG_POUR_ACTIVE] == 0.0f) return;

@@ -19,7 +19,7 @@ __all__ = [
     "LatticeConfig", "ParticleConfig", "GB300LBMSolver", "UnifiedLBMSolver",
     "create_unified_solver", "CoffeeParticleSystem", "OutflowAdjoint", "outflow_loss",
     "LBMSolverProtocol", "ParticleCoupledLBMProtocol", "validate_lbm_solver",
-    "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter",
+    "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter", "FilterPaperSystem",
 ]
 
 
@@ -41,6 +41,9 @@ def __getattr__(name):
     if name in ("LBMDiagnostics", "SnapshotWriter"):
         from . import diagnostics
         return getattr(diagnostics, name)
+    if name == "FilterPaperSystem":
+        from .filter import FilterPaperSystem
+        return FilterPaperSystem
     if name == "SlabLattice":
         from .slabs import SlabLattice
         return SlabLattice

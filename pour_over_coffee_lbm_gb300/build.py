@@ -28,6 +28,7 @@ SOURCES = {
     "adjoint.cu": [],
     "pour.cu": [],
     "diag.cu": [],
+    "filter.cu": ["-fmad=false"],
 }
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

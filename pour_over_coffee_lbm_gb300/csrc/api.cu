@@ -81,6 +81,7 @@ KParams make_kparams(const pog_params* p) {
   for (int i = 0; i < POG_INLET_NCOEF; ++i) k.coef[i] = p->inlet_coef[i];
   k.inlet_ctl = p->inlet_control;
   k.pour = p->pour_control;
+  k.blockage = p->filter_blockage;
   return k;
 }
 

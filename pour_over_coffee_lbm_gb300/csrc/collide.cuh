@@ -241,19 +241,25 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
       C r = (C)kp.eps0 / e;
       CF = (C)kp.CF0 * (r * sqrt(r));
     }
-    C sK = sqrt(K);
-    C nu0 = (C)kp.nu0;
+    // Darcy nu/K and Forchheimer C_F/sqrt(K) coefficients, both scaled by the filter
+    // blockage factor 1 + b when a blockage field is given
+    C dk = (C)kp.nu0 / K, fk = CF / sqrt(K);
+    if (kp.blockage) {
+      const C bf = (C)1 + (C)kp.blockage[c];
+      dk *= bf;
+      fk *= bf;
+    }
     if (kp.drag_mode == POG_DRAG_SEMI_IMPLICIT) {
       // Guo & Zhao 2002: u (A + nu/(2K) + C_F|u|/(2 sqrt K)) = v, solved in closed form.
-      C c0 = (C)0.5 * (A + (C)0.5 * nu0 / K);
-      C c1 = (C)0.5 * CF / sK;
+      C c0 = (C)0.5 * (A + (C)0.5 * dk);
+      C c1 = (C)0.5 * fk;
       C vm = sqrt(ux * ux + uy * uy + uz * uz);
       C s = (C)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
       ux *= s;
       uy *= s;
       uz *= s;
       C um = sqrt(ux * ux + uy * uy + uz * uz);
-      C coef = rho * (nu0 / K + CF / sK * um) + Kp;
+      C coef = rho * (dk + fk * um) + Kp;
       Fx = Gx + Kvx - coef * ux;
       Fy = Gy + Kvy - coef * uy;
       Fz = Gz + Kvz - coef * uz;
@@ -262,7 +268,7 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
       uy /= A;
       uz /= A;
       C vm = sqrt(ux * ux + uy * uy + uz * uz);
-      C coef = rho * (nu0 / K + CF / sK * vm);
+      C coef = rho * (dk + fk * vm);
       C dx = -coef * ux, dy = -coef * uy, dz = -coef * uz;
       C dm = sqrt(dx * dx + dy * dy + dz * dz);
       C cap = (C)kp.drag_cap;

@@ -62,6 +62,7 @@ struct KParams {
   float coef[POG_INLET_NCOEF];
   const float* inlet_ctl;  // device [u_inlet, a_0..a_15] or null
   const float* pour;       // device pour-nozzle block (POG_POUR_*) or null
+  const float* blockage;   // device filter-paper blockage b [n] or null
 };
 
 KParams make_kparams(const pog_params* p);

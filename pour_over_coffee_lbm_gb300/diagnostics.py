@@ -254,10 +254,10 @@ class SnapshotWriter:
             self._thread = None
 
 
-def save_checkpoint(path: str, solver, particles=None, pour=None) -> None:
+def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None) -> None:
     """Everything a run needs to continue bit for bit: the raw distribution buffer in its
     storage format, time index, flags, porosity, explicit force, LES velocity buffers, and the
-    particle and pour-nozzle state."""
+    particle, pour-nozzle and filter-paper state."""
     s = solver
     d = {"t": np.int64(s.t), "step_count": np.int64(s.step_count), "storage": np.int32(s.cfg.storage),
          "shape": np.array([s.NX, s.NY, s.NZ], np.int64),
@@ -280,12 +280,16 @@ def save_checkpoint(path: str, solver, particles=None, pour=None) -> None:
                   "p_since_sort": np.int64(-1 if p._since_sort is None else p._since_sort)})
     if pour is not None:
         d["pour"] = pour.block.cpu().numpy()
+    if filter_system is not None:
+        d.update({"filter_accum": filter_system.accumulated_particles.cpu().numpy(),
+                  "filter_blockage": filter_system.filter_blockage.cpu().numpy(),
+                  "filter_step": np.int64(filter_system.step_count), "filter_seed": np.int64(filter_system.seed)})
     tmp = path + ".tmp.npz"
     np.savez(tmp, **d)
     os.replace(tmp, path)
 
 
-def load_checkpoint(path: str, solver, particles=None, pour=None) -> None:
+def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None) -> None:
     """Restore a save_checkpoint file into objects built with the same configuration."""
     s = solver
     z = np.load(path)
@@ -316,3 +320,8 @@ def load_checkpoint(path: str, solver, particles=None, pour=None) -> None:
         p._since_sort = None if ss < 0 else ss
     if pour is not None and "pour" in z:
         pour.block.copy_(torch.from_numpy(z["pour"]))
+    if filter_system is not None and "filter_accum" in z:
+        filter_system.accumulated_particles.copy_(torch.from_numpy(z["filter_accum"]))
+        filter_system.filter_blockage.copy_(torch.from_numpy(z["filter_blockage"]))
+        filter_system.step_count = int(z["filter_step"])
+        filter_system.seed = int(z["filter_seed"])

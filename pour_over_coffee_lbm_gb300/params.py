@@ -43,6 +43,7 @@ class PogParams(ctypes.Structure):
         ("rho_outlet", ctypes.c_float),
         ("inlet_control", ctypes.c_void_p),
         ("pour_control", ctypes.c_void_p),
+        ("filter_blockage", ctypes.c_void_p),
     ]
 
 

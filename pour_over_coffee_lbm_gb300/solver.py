@@ -163,6 +163,7 @@ class GB300LBMSolver:
         self._porosity = None
         self._inlet_ctl = None
         self._pour_ctl = None
+        self._blockage = None
         if porosity is not None:
             self.set_porosity(porosity)
         self.t = 0
@@ -428,15 +429,15 @@ class GB300LBMSolver:
         self._inlet_ctl = control
         self._p.inlet_control = None if control is None else control.data_ptr()
 
-    def save_checkpoint(self, path: str, particles=None, pour=None) -> None:
-        """Raw state of the run (and of its particles / pour nozzle) to an .npz file that
-        load_checkpoint continues bit for bit."""
+    def save_checkpoint(self, path: str, particles=None, pour=None, filter_system=None) -> None:
+        """Raw state of the run (and of its particles / pour nozzle / filter paper) to an .npz
+        file that load_checkpoint continues bit for bit."""
         from .diagnostics import save_checkpoint
-        save_checkpoint(path, self, particles, pour)
+        save_checkpoint(path, self, particles, pour, filter_system)
 
-    def load_checkpoint(self, path: str, particles=None, pour=None) -> None:
+    def load_checkpoint(self, path: str, particles=None, pour=None, filter_system=None) -> None:
         from .diagnostics import load_checkpoint
-        load_checkpoint(path, self, particles, pour)
+        load_checkpoint(path, self, particles, pour, filter_system)
 
     def set_pour_control(self, block: Optional[torch.Tensor]) -> None:
         """Attach a pour-nozzle block (PrecisePouringSystem.block: CUDA float32, POG_POUR_NFIELDS
@@ -446,6 +447,18 @@ class GB300LBMSolver:
                 raise ValueError("pour block must be a contiguous CUDA float32 tensor of 20 values")
         self._pour_ctl = block
         self._p.pour_control = None if block is None else block.data_ptr()
+        self._macro_dirty = True
+
+    def set_filter_blockage(self, blockage: Optional[torch.Tensor]) -> None:
+        """Attach the filter-paper blockage field b (CUDA float32, one value per cell, written by
+        FilterPaperSystem): porous cells scale their Darcy and Forchheimer coefficients by
+        (1 + b).  None detaches it."""
+        if blockage is not None:
+            if (blockage.dtype != torch.float32 or blockage.numel() != self.n or not blockage.is_cuda
+                    or not blockage.is_contiguous()):
+                raise ValueError("filter blockage must be a contiguous CUDA float32 tensor of ncell values")
+        self._blockage = blockage
+        self._p.filter_blockage = None if blockage is None else blockage.data_ptr()
         self._macro_dirty = True
 
     def capture(self, nsteps: int, particle_system=None, dt: float = 1.0,
