@@ -215,6 +215,18 @@ int pog_filter_particles(const pog_params* p, const uint32_t* flags, const float
 int pog_filter_update(const pog_params* p, const uint32_t* flags, float* accum, float* blockage,
                       void* stream);
 
+/* ---- pressure-gradient drive (PressureGradientDrive, src/physics/pressure_gradient_drive.py) ---- */
+/* force[a][c] += scale * F_a(c) for every non-solid cell, F = -c_s^2 grad(rho) / rho (central
+ * differences, one-sided on the domain faces; 0 where rho <= 1e-12), capped at |F| <= max_force
+ * (compute_pressure_gradient :124-177; scale 1 = force drive :188-193, 0.5 = mixed drive
+ * :274-279).  rho [ncell], force [3][ncell], natural order, DEVICE pointers. */
+int pog_pressure_force(const pog_params* p, const uint32_t* flags, const float* rho, float* force,
+                       float scale, float max_force, void* stream);
+/* rho[c] := clamp(rho[c] + clamp((target[k] - rho[c]) * rate, +-max_adjust), rho_min, rho_max)
+ * for every non-solid cell, target [nz] per plane (apply_density_drive :95-122). */
+int pog_density_drive(const pog_params* p, const uint32_t* flags, float* rho, const float* target,
+                      float rate, float max_adjust, float rho_min, float rho_max, void* stream);
+
 /* ---- diagnostics ----------------------------------------------------------------------------- */
 /* Field statistics of rho [ncell] and u [3][ncell] (FP32, every cell of the grid, as the
  * reference's host-side LBMDiagnostics computes them from to_numpy() copies,

@@ -52,6 +52,8 @@ def load():
             lib.orc_pour_advance.restype = None
             lib.orc_filter_particles.restype = None
             lib.orc_filter_update.restype = None
+            lib.orc_pressure_force.restype = None
+            lib.orc_density_drive.restype = None
             lib.orc_pour_advance.argtypes = [_v, _v]
             _lib = lib
         return _lib
@@ -84,6 +86,24 @@ def filter_update(cfg, flags, accum, blockage):
     lib = load()
     _, pp = _params(cfg)
     lib.orc_filter_update(pp, _p(flags), _p(accum), _p(blockage))
+
+
+def pressure_force(cfg, flags, rho, force, scale, max_force):
+    """Pressure-gradient force added in place to force (float32 [3][ncell])."""
+    for a, dt in ((flags, np.uint32), (rho, np.float32), (force, np.float32)):
+        assert a.dtype == dt and a.flags.c_contiguous
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_pressure_force(pp, _p(flags), _p(rho), _p(force), ctypes.c_float(scale), ctypes.c_float(max_force))
+
+
+def density_drive(cfg, flags, rho, target, rate, max_adjust, lo, hi):
+    """Density relaxation toward target [nz], in place on rho (float32 [ncell])."""
+    for a, dt in ((flags, np.uint32), (rho, np.float32), (target, np.float32)):
+        assert a.dtype == dt and a.flags.c_contiguous
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_density_drive(pp, _p(flags), _p(rho), _p(target), *(ctypes.c_float(v) for v in (rate, max_adjust, lo, hi)))
 
 
 def pour_advance(cfg, pour):

@@ -667,6 +667,57 @@ void orc_filter_update(const pog_params* p, const uint32_t* flags, float* accum,
   }
 }
 
+// Pressure-gradient drive (pressure_gradient_drive.py:95-193), the library's drive.cu restated.
+void orc_pressure_force(const pog_params* p, const uint32_t* flags, const float* rho, float* force, float scale,
+                        float max_force) {
+  const long long nx = p->nx, ny = p->ny, nz = p->nz, n = nx * ny * nz, pl = nx * ny;
+  for (long long k = 0; k < nz; ++k)
+    for (long long j = 0; j < ny; ++j)
+      for (long long i = 0; i < nx; ++i) {
+        const long long c = (k * ny + j) * nx + i;
+        if (flags[c] & POG_CELL_SOLID) continue;
+        const float r = rho[c];
+        float gx, gy, gz;
+        if (i > 0 && i < nx - 1) gx = (rho[c + 1] - rho[c - 1]) * 0.5f;
+        else if (i == 0) gx = rho[c + 1] - r;
+        else gx = r - rho[c - 1];
+        if (j > 0 && j < ny - 1) gy = (rho[c + nx] - rho[c - nx]) * 0.5f;
+        else if (j == 0) gy = rho[c + nx] - r;
+        else gy = r - rho[c - nx];
+        if (k > 0 && k < nz - 1) gz = (rho[c + pl] - rho[c - pl]) * 0.5f;
+        else if (k == 0) gz = rho[c + pl] - r;
+        else gz = r - rho[c - pl];
+        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+        if (r > 1e-12f) {
+          const float cs2 = 1.0f / 3.0f;
+          fx = -(gx * cs2) / r;
+          fy = -(gy * cs2) / r;
+          fz = -(gz * cs2) / r;
+          const float m = sqrtf(fx * fx + fy * fy + fz * fz);
+          if (m > max_force) {
+            const float s = max_force / m;
+            fx *= s;
+            fy *= s;
+            fz *= s;
+          }
+        }
+        force[c] += scale * fx;
+        force[n + c] += scale * fy;
+        force[2 * n + c] += scale * fz;
+      }
+}
+void orc_density_drive(const pog_params* p, const uint32_t* flags, float* rho, const float* target, float rate,
+                       float max_adjust, float lo, float hi) {
+  const long long pl = (long long)p->nx * p->ny, n = pl * p->nz;
+  for (long long c = 0; c < n; ++c) {
+    if (flags[c] & POG_CELL_SOLID) continue;
+    const float r = rho[c];
+    float a = (target[c / pl] - r) * rate;
+    if (fabsf(a) > max_adjust) a = a > 0.0f ? max_adjust : -max_adjust;
+    rho[c] = std::max(lo, std::min(hi, r + a));
+  }
+}
+
 // One nozzle step of a host pour block (pour_advance_kernel in the library).
 void orc_pour_advance(const pog_params* p, float* b) {
   if (b[POG_POUR_ACTIVE] == 0.0f) return;

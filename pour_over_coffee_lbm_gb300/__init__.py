@@ -20,6 +20,7 @@ __all__ = [
     "create_unified_solver", "CoffeeParticleSystem", "OutflowAdjoint", "outflow_loss",
     "LBMSolverProtocol", "ParticleCoupledLBMProtocol", "validate_lbm_solver",
     "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter", "FilterPaperSystem",
+    "PressureGradientDrive",
 ]
 
 
@@ -41,6 +42,9 @@ def __getattr__(name):
     if name in ("LBMDiagnostics", "SnapshotWriter"):
         from . import diagnostics
         return getattr(diagnostics, name)
+    if name == "PressureGradientDrive":
+        from .drive import PressureGradientDrive
+        return PressureGradientDrive
     if name == "FilterPaperSystem":
         from .filter import FilterPaperSystem
         return FilterPaperSystem

@@ -34,6 +34,8 @@ SIGNATURES = [
     ("pog_field_stats", _i, [_P, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_filter_particles", _i, [_P, _v, _v, _v, _v, _i, _v, ctypes.c_uint32, _ll, _v]),
     ("pog_filter_update", _i, [_P, _v, _v, _v, _v]),
+    ("pog_pressure_force", _i, [_P, _v, _v, _v, _f, _f, _v]),
+    ("pog_density_drive", _i, [_P, _v, _v, _v, _f, _f, _f, _f, _v]),
     ("pog_step", _i, [_P, _v, _v, _ll, _i, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_step_push", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_export_natural", _i, [_P, _v, _v, _ll, _v, _i, _v]),

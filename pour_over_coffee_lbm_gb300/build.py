@@ -29,6 +29,7 @@ SOURCES = {
     "pour.cu": [],
     "diag.cu": [],
     "filter.cu": ["-fmad=false"],
+    "drive.cu": ["-fmad=false"],
 }
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
