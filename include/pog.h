@@ -127,6 +127,12 @@ typedef struct pog_params {
    * NULL: porous cells scale their Darcy and Forchheimer coefficients by (1 + b[c])
    * (apply_filter_effects' blockage_factor, filter_paper.py:584-587). */
   const float* filter_blockage;
+  /* Optional DEVICE pointer to the phase indicator [ncell] (lbm.phase: 0 = air, 1 = water) or
+   * NULL (water everywhere).  Per cell (legacy/lbm_solver.py:558-592, les_turbulence.py:362-366):
+   * gravity rho*g*phase where phase > 0.001 and none elsewhere; tau = tau where phase > 0.5,
+   * else tau_air; nu_sgs = 0 where |phase| < 0.9. */
+  const float* phase;
+  float tau_air;            /* molecular relaxation time of the air phase (TAU_AIR)           */
 } pog_params;
 
 /* Pour-nozzle block, floats (PrecisePouringSystem, src/physics/precise_pouring.py:12-193):
@@ -214,6 +220,40 @@ int pog_filter_particles(const pog_params* p, const uint32_t* flags, const float
  * b := 0.95 b + 0.05 * 0.9 (1 - exp(-0.1 accum)), accum := 0.999 accum. */
 int pog_filter_update(const pog_params* p, const uint32_t* flags, float* accum, float* blockage,
                       void* stream);
+
+/* ---- multiphase phase field (MultiphaseFlow3D, src/core/multiphase_3d.py) ------------------- */
+/* phi [ncell] in [-1, 1] (-1 air, +1 water), natural order, DEVICE pointers.  The stencil passes
+ * touch interior cells only (1 <= i < nx-1, ...); fields they write keep their outer shell. */
+/* mu = phi^3 - phi - kappa lap(phi) (compute_chemical_potential :80-109). */
+int pog_phase_chemical_potential(const pog_params* p, const float* phi, float kappa, float* mu,
+                                 void* stream);
+/* normal [3][ncell] = grad(phi)/|grad(phi)| (0 where |grad| <= 1e-10), gmag [ncell] = |grad|
+ * (compute_gradients :111-132).  Allocate both zeroed: the shell is never written. */
+int pog_phase_normals(const pog_params* p, const float* phi, float* normal, float* gmag,
+                      void* stream);
+/* Curvature kappa = div(normal) (:134-149) and the surface-tension force F = sigma kappa |grad|
+ * normal where |phi| < 0.9 (:313-331).  body_force (nullable, needs rho): += F / rho on non-solid
+ * cells with rho > 1e-10 (apply_surface_tension :354-363).  curvature [ncell] and surface_force
+ * [3][ncell] are optional outputs. */
+int pog_phase_surface_tension(const pog_params* p, const uint32_t* flags, const float* phi,
+                              const float* normal, const float* gmag, const float* rho,
+                              float sigma, float* body_force, float* curvature,
+                              float* surface_force, void* stream);
+/* One phase-field step into phi_new (phi_new != phi): upwind advection by u [3][ncell] (zero in
+ * solid cells) + mobility lap(mu) (mu NULL = 0), clamp to [-1, 1], then the phase-separation
+ * relaxation where |phi| < 0.99 (:151-197, :334-352); non-interior cells carry phi over.  With
+ * rho and phase (both or neither): rho = rho_air + (rho_water - rho_air)(phi' + 1)/2 and
+ * phase = (phi' + 1)/2 from the clamped new phi' (update_density_from_phase :365-381). */
+int pog_phase_update(const pog_params* p, const uint32_t* flags, const float* phi, float* phi_new,
+                     const float* u, const float* mu, float mobility, float dt, float rho_air,
+                     float rho_water, float* rho, float* phase, void* stream);
+/* rho and phase from phi alone (update_density_from_phase :365-381). */
+int pog_phase_properties(const pog_params* p, const float* phi, float rho_air, float rho_water,
+                         float* rho, float* phase, void* stream);
+/* The pour stream's phase change (apply_gradual_phase_change, precise_pouring.py:166-193): in the
+ * stream of p->pour_control, non-solid cells move toward water by
+ * clamp((1 - phi)/0.05, +-2) * intensity * dt * flow, clamped to [-1, 1]. */
+int pog_pour_phase(const pog_params* p, const uint32_t* flags, float* phi, float dt, void* stream);
 
 /* ---- pressure-gradient drive (PressureGradientDrive, src/physics/pressure_gradient_drive.py) ---- */
 /* force[a][c] += scale * F_a(c) for every non-solid cell, F = -c_s^2 grad(rho) / rho (central
@@ -370,7 +410,7 @@ int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* 
  *   cell adds dJ/df_i = -c_iz.  Parameter gradients are accumulated in FP64:
  *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
  *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL,
- *   pour_control and filter_blockage NULL (POG_E_ARG otherwise). */
+ *   pour_control, filter_blockage and phase NULL (POG_E_ARG otherwise). */
 int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next, void* lam_t,
                      const uint32_t* flags, const float* porosity, double* grad_porosity,
                      double* grad_inlet, void* stream);

@@ -54,6 +54,9 @@ def load():
             lib.orc_filter_update.restype = None
             lib.orc_pressure_force.restype = None
             lib.orc_density_drive.restype = None
+            for name in ("orc_phase_chemical_potential", "orc_phase_normals", "orc_phase_surface_tension",
+                         "orc_phase_update", "orc_phase_properties", "orc_pour_phase"):
+                getattr(lib, name).restype = None
             lib.orc_pour_advance.argtypes = [_v, _v]
             _lib = lib
         return _lib
@@ -106,6 +109,60 @@ def density_drive(cfg, flags, rho, target, rate, max_adjust, lo, hi):
     lib.orc_density_drive(pp, _p(flags), _p(rho), _p(target), *(ctypes.c_float(v) for v in (rate, max_adjust, lo, hi)))
 
 
+def _f32(*arrays):
+    for a in arrays:
+        if a is not None:
+            assert a.dtype == np.float32 and a.flags.c_contiguous
+
+
+def phase_chemical_potential(cfg, phi, kappa, mu):
+    _f32(phi, mu)
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_phase_chemical_potential(pp, _p(phi), ctypes.c_float(kappa), _p(mu))
+
+
+def phase_normals(cfg, phi, normal, gmag):
+    _f32(phi, normal, gmag)
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_phase_normals(pp, _p(phi), _p(normal), _p(gmag))
+
+
+def phase_surface_tension(cfg, flags, phi, normal, gmag, rho, sigma, body_force=None, curvature=None,
+                          surface_force=None):
+    _f32(phi, normal, gmag, rho, body_force, curvature, surface_force)
+    assert flags.dtype == np.uint32
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_phase_surface_tension(pp, _p(flags), _p(phi), _p(normal), _p(gmag), _p(rho), ctypes.c_float(sigma),
+                                  _p(body_force), _p(curvature), _p(surface_force))
+
+
+def phase_update(cfg, flags, phi, phi_new, u, mu, mobility, dt, rho_air, rho_water, rho=None, phase=None):
+    _f32(phi, phi_new, u, mu, rho, phase)
+    assert flags.dtype == np.uint32
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_phase_update(pp, _p(flags), _p(phi), _p(phi_new), _p(u), _p(mu),
+                         *(ctypes.c_float(v) for v in (mobility, dt, rho_air, rho_water)), _p(rho), _p(phase))
+
+
+def phase_properties(cfg, phi, rho_air, rho_water, rho, phase):
+    _f32(phi, rho, phase)
+    lib = load()
+    _, pp = _params(cfg)
+    lib.orc_phase_properties(pp, _p(phi), ctypes.c_float(rho_air), ctypes.c_float(rho_water), _p(rho), _p(phase))
+
+
+def pour_phase(cfg, flags, phi, dt, pour):
+    _f32(phi, pour)
+    assert flags.dtype == np.uint32
+    lib = load()
+    _, pp = _params(cfg, pour)
+    lib.orc_pour_phase(pp, _p(flags), _p(phi), ctypes.c_float(dt))
+
+
 def pour_advance(cfg, pour):
     """One nozzle step of a host pour block, in place."""
     lib = load()
@@ -142,15 +199,18 @@ def init_equilibrium(cfg, flags, dtype=np.float64, rho0=None, u0=(0.0, 0.0, 0.0)
 
 
 def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdrag=None, pour=None,
-         blockage=None):
+         blockage=None, phase=None):
     """One push step.  force: [3][n] explicit force; pdrag: [4][n] particle drag deposit
-    (Kp, Kv); pour: host pour-nozzle block; blockage: [n] filter blockage.  Returns
-    (f_next, rho, u)."""
+    (Kp, Kv); pour: host pour-nozzle block; blockage: [n] filter blockage; phase: [n] phase
+    indicator (0 air, 1 water).  Returns (f_next, rho, u)."""
     lib = load()
     _keep, pp = _params(cfg, pour)
     if blockage is not None:
         blockage = np.ascontiguousarray(blockage, np.float32)
         _keep.filter_blockage = blockage.ctypes.data_as(ctypes.c_void_p).value
+    if phase is not None:
+        phase = np.ascontiguousarray(phase, np.float32)
+        _keep.phase = phase.ctypes.data_as(ctypes.c_void_p).value
     dt = f.dtype
     fo = f.copy()
     rho = np.zeros((cfg.nz, cfg.ny, cfg.nx), dt)

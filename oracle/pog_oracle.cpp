@@ -234,7 +234,11 @@ void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int
     equilibrium<T>((T)p->rho_outlet, ux, uy, uz, fs);
     if (red) red[POG_RED_OUTFLOW] += -(double)mz;
   } else {
-    T Gx = rho * (T)p->gx, Gy = rho * (T)p->gy, Gz = rho * (T)p->gz;
+    // phase indicator (HOST array for the restatement): gravity on the water fraction,
+    // tau by phase, LES gate |phase| < 0.9 (legacy/lbm_solver.py:558-592, les_turbulence.py:362-366)
+    const T ph = p->phase ? (T)p->phase[g.idx(i, j, k)] : (T)1;
+    const T rg = p->phase ? (ph > (T)0.001 ? rho * ph : (T)0) : rho;
+    T Gx = rg * (T)p->gx, Gy = rg * (T)p->gy, Gz = rg * (T)p->gz;
     if (Fe) {
       Gx += Fe[0];
       Gy += Fe[1];
@@ -314,9 +318,10 @@ void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int
       Fz = Gz + Kvz - Kp * uz;
     }
     equilibrium<T>(rho, ux, uy, uz, feq);
-    T tau0 = (T)p->tau;
+    T tau0 = p->phase ? (ph > (T)0.5 ? (T)p->tau : (T)p->tau_air) : (T)p->tau;
+    const bool les_on = !porous && !(p->phase && ph < (T)0.9 && ph > (T)-0.9);
     T nu = 0;
-    if (!porous && p->les_mode == POG_LES_LOCAL) {
+    if (les_on && p->les_mode == POG_LES_LOCAL) {
       T P[6] = {0, 0, 0, 0, 0, 0};  // xx yy zz xy xz yz
       for (int q = 0; q < 19; ++q) {
         T d = f[q] - feq[q];
@@ -336,7 +341,7 @@ void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int
       nu = (tl - tau0) / (T)3;
       if (smag < (T)p->les_strain_floor) nu = 0;
       nu = std::min(nu, (T)p->les_nu_max);
-    } else if (!porous && p->les_mode == POG_LES_STENCIL) {
+    } else if (les_on && p->les_mode == POG_LES_STENCIL) {
       nu = nu_stencil;
     }
     T tau = tau0 + (T)3 * nu;
@@ -716,6 +721,162 @@ void orc_density_drive(const pog_params* p, const uint32_t* flags, float* rho, c
     if (fabsf(a) > max_adjust) a = a > 0.0f ? max_adjust : -max_adjust;
     rho[c] = std::max(lo, std::min(hi, r + a));
   }
+}
+
+// Multiphase phase field (multiphase_3d.py:80-381) and the pour stream's phase change
+// (precise_pouring.py:166-193), the library's multiphase.cu restated.
+struct PG {
+  long long nx, ny, nz, pl, n;
+  bool interior(long long c) const {
+    const long long i = c % nx, j = (c / nx) % ny, k = c / pl;
+    return i >= 1 && i + 1 < nx && j >= 1 && j + 1 < ny && k >= 1 && k + 1 < nz;
+  }
+  float lap7(const float* a, long long c) const {
+    return a[c + 1] + a[c - 1] + a[c + nx] + a[c - nx] + a[c + pl] + a[c - pl] - 6.0f * a[c];
+  }
+};
+static PG pgrid(const pog_params* p) {
+  PG g;
+  g.nx = p->nx;
+  g.ny = p->ny;
+  g.nz = p->nz;
+  g.pl = g.nx * g.ny;
+  g.n = g.pl * g.nz;
+  return g;
+}
+void orc_phase_chemical_potential(const pog_params* p, const float* phi, float kappa, float* mu) {
+  const PG g = pgrid(p);
+  for (long long c = 0; c < g.n; ++c) {
+    if (!g.interior(c)) continue;
+    const float ph = phi[c];
+    const float lap = g.lap7(phi, c);
+    mu[c] = (ph * ph * ph - ph) + (-kappa * lap);
+  }
+}
+void orc_phase_normals(const pog_params* p, const float* phi, float* normal, float* gmag) {
+  const PG g = pgrid(p);
+  for (long long c = 0; c < g.n; ++c) {
+    if (!g.interior(c)) continue;
+    const float gx = (phi[c + 1] - phi[c - 1]) * 0.5f;
+    const float gy = (phi[c + g.nx] - phi[c - g.nx]) * 0.5f;
+    const float gz = (phi[c + g.pl] - phi[c - g.pl]) * 0.5f;
+    const float m = sqrtf(gx * gx + gy * gy + gz * gz);
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (m > 1e-10f) {
+      nx = gx / m;
+      ny = gy / m;
+      nz = gz / m;
+    }
+    normal[c] = nx;
+    normal[g.n + c] = ny;
+    normal[2 * g.n + c] = nz;
+    gmag[c] = m;
+  }
+}
+void orc_phase_surface_tension(const pog_params* p, const uint32_t* flags, const float* phi, const float* normal,
+                               const float* gmag, const float* rho, float sigma, float* body_force, float* curvature,
+                               float* sforce) {
+  const PG g = pgrid(p);
+  for (long long c = 0; c < g.n; ++c) {
+    if (!g.interior(c)) continue;
+    const float m = gmag[c];
+    float kap = 0.0f;
+    if (m > 1e-10f)
+      kap = (normal[c + 1] - normal[c - 1]) * 0.5f + (normal[g.n + c + g.nx] - normal[g.n + c - g.nx]) * 0.5f +
+            (normal[2 * g.n + c + g.pl] - normal[2 * g.n + c - g.pl]) * 0.5f;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    if (fabsf(phi[c]) < 0.9f && m > 1e-10f) {
+      const float fm = sigma * kap * m;
+      fx = fm * normal[c];
+      fy = fm * normal[g.n + c];
+      fz = fm * normal[2 * g.n + c];
+    }
+    if (curvature) curvature[c] = kap;
+    if (sforce) {
+      sforce[c] = fx;
+      sforce[g.n + c] = fy;
+      sforce[2 * g.n + c] = fz;
+    }
+    if (body_force && !(flags[c] & POG_CELL_SOLID) && rho[c] > 1e-10f) {
+      body_force[c] += fx / rho[c];
+      body_force[g.n + c] += fy / rho[c];
+      body_force[2 * g.n + c] += fz / rho[c];
+    }
+  }
+}
+void orc_phase_update(const pog_params* p, const uint32_t* flags, const float* phi, float* phi_new, const float* u,
+                      const float* mu, float mobility, float dt, float rho_air, float rho_water, float* rho,
+                      float* phase) {
+  const PG g = pgrid(p);
+  const float drho = (float)((double)rho_water - (double)rho_air);
+  for (long long c = 0; c < g.n; ++c) {
+    const float ph = phi[c];
+    float pn = ph;
+    if (g.interior(c)) {
+      float ux = 0.0f, uy = 0.0f, uz = 0.0f;
+      if (!(flags[c] & POG_CELL_SOLID)) {
+        ux = u[c];
+        uy = u[g.n + c];
+        uz = u[2 * g.n + c];
+      }
+      const float dx = ux > 0.0f ? ph - phi[c - 1] : phi[c + 1] - ph;
+      const float dy = uy > 0.0f ? ph - phi[c - g.nx] : phi[c + g.nx] - ph;
+      const float dz = uz > 0.0f ? ph - phi[c - g.pl] : phi[c + g.pl] - ph;
+      const float conv = -(ux * dx + uy * dy + uz * dz);
+      float diff = 0.0f;
+      if (mu) diff = mobility * g.lap7(mu, c);
+      pn = ph + dt * (conv + diff);
+      pn = std::max(-1.0f, std::min(1.0f, pn));
+      if (fabsf(ph) < 0.99f) {
+        const float lap = g.lap7(phi, c);
+        const float chem = ph * (ph * ph - 1.0f) - 0.01f * lap;
+        pn = pn + -0.001f * chem * dt;
+      }
+    }
+    phi_new[c] = pn;
+    if (rho) {
+      const float pc = std::max(-1.0f, std::min(1.0f, pn));
+      rho[c] = rho_air + drho * (pc + 1.0f) / 2.0f;
+      phase[c] = (pc + 1.0f) / 2.0f;
+    }
+  }
+}
+void orc_phase_properties(const pog_params* p, const float* phi, float rho_air, float rho_water, float* rho,
+                          float* phase) {
+  const PG g = pgrid(p);
+  const float drho = (float)((double)rho_water - (double)rho_air);
+  for (long long c = 0; c < g.n; ++c) {
+    const float pc = std::max(-1.0f, std::min(1.0f, phi[c]));
+    rho[c] = rho_air + drho * (pc + 1.0f) / 2.0f;
+    phase[c] = (pc + 1.0f) / 2.0f;
+  }
+}
+void orc_pour_phase(const pog_params* p, const uint32_t* flags, float* phi, float dt) {
+  const float* b = p->pour_control;  // HOST block for the restatement
+  if (!b || b[POG_POUR_ACTIVE] == 0.0f) return;
+  const PG g = pgrid(p);
+  const float ztop = b[POG_POUR_ZTOP];
+  const float klo = ceilf(ztop - b[POG_POUR_HEIGHT]), khi = floorf(ztop);
+  if (!(khi >= 0.0f) || klo > (float)(g.nz - 1) || khi < klo) return;
+  const long long k0 = (long long)std::max(klo, 0.0f), k1 = (long long)std::min(khi, (float)(g.nz - 1));
+  const float R = b[POG_POUR_RADIUS], px = b[POG_POUR_X], py = b[POG_POUR_Y], flow = b[POG_POUR_FLOW];
+  for (long long k = k0; k <= k1; ++k)
+    for (long long j = 0; j < g.ny; ++j)
+      for (long long i = 0; i < g.nx; ++i) {
+        const long long c = k * g.pl + j * g.nx + i;
+        if (flags[c] & POG_CELL_SOLID) continue;
+        const float dx = (float)i - px, dy = (float)j - py;
+        const float d = sqrtf(dx * dx + dy * dy);
+        if (!(d <= R)) continue;
+        const float dr = d / R;
+        const float I = expf(-0.5f * dr * dr) * expf(-(ztop - (float)k) / 2.0f);
+        if (!(I > 0.0f)) continue;
+        const float cur = phi[c];
+        float rate = (1.0f - cur) / 0.05f;
+        rate = std::max(-2.0f, std::min(2.0f, rate));
+        const float nw = cur + rate * I * dt * flow;
+        phi[c] = std::max(-1.0f, std::min(1.0f, nw));
+      }
 }
 
 // One nozzle step of a host pour block (pour_advance_kernel in the library).

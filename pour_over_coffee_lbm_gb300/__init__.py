@@ -20,7 +20,7 @@ __all__ = [
     "create_unified_solver", "CoffeeParticleSystem", "OutflowAdjoint", "outflow_loss",
     "LBMSolverProtocol", "ParticleCoupledLBMProtocol", "validate_lbm_solver",
     "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter", "FilterPaperSystem",
-    "PressureGradientDrive",
+    "PressureGradientDrive", "MultiphaseFlow3D",
 ]
 
 
@@ -42,6 +42,9 @@ def __getattr__(name):
     if name in ("LBMDiagnostics", "SnapshotWriter"):
         from . import diagnostics
         return getattr(diagnostics, name)
+    if name == "MultiphaseFlow3D":
+        from .multiphase import MultiphaseFlow3D
+        return MultiphaseFlow3D
     if name == "PressureGradientDrive":
         from .drive import PressureGradientDrive
         return PressureGradientDrive

@@ -36,6 +36,12 @@ SIGNATURES = [
     ("pog_filter_update", _i, [_P, _v, _v, _v, _v]),
     ("pog_pressure_force", _i, [_P, _v, _v, _v, _f, _f, _v]),
     ("pog_density_drive", _i, [_P, _v, _v, _v, _f, _f, _f, _f, _v]),
+    ("pog_phase_chemical_potential", _i, [_P, _v, _f, _v, _v]),
+    ("pog_phase_normals", _i, [_P, _v, _v, _v, _v]),
+    ("pog_phase_surface_tension", _i, [_P, _v, _v, _v, _v, _v, _f, _v, _v, _v, _v]),
+    ("pog_phase_update", _i, [_P, _v, _v, _v, _v, _v, _f, _f, _f, _f, _v, _v, _v]),
+    ("pog_phase_properties", _i, [_P, _v, _f, _f, _v, _v, _v]),
+    ("pog_pour_phase", _i, [_P, _v, _v, _f, _v]),
     ("pog_step", _i, [_P, _v, _v, _ll, _i, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_step_push", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_export_natural", _i, [_P, _v, _v, _ll, _v, _i, _v]),

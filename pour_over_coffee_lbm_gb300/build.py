@@ -30,6 +30,7 @@ SOURCES = {
     "diag.cu": [],
     "filter.cu": ["-fmad=false"],
     "drive.cu": ["-fmad=false"],
+    "multiphase.cu": ["-fmad=false"],
 }
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -386,8 +386,8 @@ extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void
   if (p->drag_mode != POG_DRAG_SEMI_IMPLICIT || p->forcing_mode != POG_FORCING_GUO || p->clamp_tau)
     return set_error(POG_E_ARG, "adjoint supports semi-implicit drag, Guo forcing, no tau clamp");
   if (grad_porosity && !porosity) return set_error(POG_E_ARG, "grad_porosity needs porosity");
-  if (p->pour_control || p->filter_blockage)
-    return set_error(POG_E_ARG, "adjoint does not differentiate the pour stream or the filter blockage");
+  if (p->pour_control || p->filter_blockage || p->phase)
+    return set_error(POG_E_ARG, "adjoint does not differentiate the pour stream, filter blockage or phase field");
   KParams kp = make_kparams(p);
   cudaStream_t s = (cudaStream_t)stream;
   if (p->storage == POG_STORE_F32)

@@ -82,6 +82,8 @@ KParams make_kparams(const pog_params* p) {
   k.inlet_ctl = p->inlet_control;
   k.pour = p->pour_control;
   k.blockage = p->filter_blockage;
+  k.phase = p->phase;
+  k.tau_air = p->tau_air;
   return k;
 }
 
@@ -117,6 +119,8 @@ int pog_validate_params(const pog_params* p) {
   if (p->forcing_mode < 0 || p->forcing_mode > 1)
     return set_error(POG_E_ARG, "forcing_mode %d unknown", p->forcing_mode);
   if (!(p->tau > 0.5f)) return set_error(POG_E_ARG, "tau=%g must be > 0.5", (double)p->tau);
+  if (p->phase && !(p->tau_air > 0.5f))
+    return set_error(POG_E_ARG, "tau_air=%g must be > 0.5 with a phase field", (double)p->tau_air);
   if (!(p->rho0 > 0.0f)) return set_error(POG_E_ARG, "rho0 must be > 0");
   if (p->band_thickness > 0) {
     if (!(p->porosity > 0.0f && p->porosity < 1.0f))

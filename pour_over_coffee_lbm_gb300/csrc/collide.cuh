@@ -209,8 +209,12 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     return res;
   }
 
+  // Phase indicator (multiphase runs): gravity acts on the water fraction only, tau follows
+  // the phase, LES is off in the interface and the air (legacy/lbm_solver.py:558-592).
+  const C ph = kp.phase ? (C)kp.phase[c] : (C)1;
   // Total non-drag force density: gravity rho*g plus the external (particle/plugin) force.
-  C Gx = rho * (C)kp.gx, Gy = rho * (C)kp.gy, Gz = rho * (C)kp.gz;
+  const C rg = kp.phase ? (ph > (C)0.001 ? rho * ph : (C)0) : rho;
+  C Gx = rg * (C)kp.gx, Gy = rg * (C)kp.gy, Gz = rg * (C)kp.gz;
   if (force) {
     Gx += (C)force[c];
     Gy += (C)force[kp.n + c];
@@ -295,9 +299,11 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     Fz = Gz + Kvz - Kp * uz;
   }
   const C usq = ux * ux + uy * uy + uz * uz;
-  const C tau0 = (C)kp.tau;
+  const C tau0 = kp.phase ? (ph > (C)0.5 ? (C)kp.tau : (C)kp.tau_air) : (C)kp.tau;
+  // the LES phase gate |phase| < 0.9 (les_turbulence.py:362-366)
+  const bool les_on = !porous && !(kp.phase && ph < (C)0.9 && ph > (C)-0.9);
   C nu = (C)0;
-  if (kp.les_mode == POG_LES_LOCAL && !porous) {
+  if (kp.les_mode == POG_LES_LOCAL && les_on) {
     // Pi_neq = sum e e f - rho (u u + I/3)
     // SH: sum e_a e_b f = rho0/3 delta_ab + sc sum e_a e_b h
     const C r3 = (SH ? drho : rho) * (C)(1.0 / 3.0);
@@ -315,7 +321,7 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
     nu = (tl - tau0) * (C)(1.0 / 3.0);
     if (smag < (C)kp.strain_floor) nu = (C)0;
     nu = nu < (C)kp.nu_max ? nu : (C)kp.nu_max;
-  } else if (kp.les_mode == POG_LES_STENCIL && !porous) {
+  } else if (kp.les_mode == POG_LES_STENCIL && les_on) {
     nu = nu_st;
   }
   C tau = tau0 + (C)3 * nu;

@@ -63,6 +63,8 @@ struct KParams {
   const float* inlet_ctl;  // device [u_inlet, a_0..a_15] or null
   const float* pour;       // device pour-nozzle block (POG_POUR_*) or null
   const float* blockage;   // device filter-paper blockage b [n] or null
+  const float* phase;      // device phase indicator [n] (0 air, 1 water) or null
+  float tau_air;
 };
 
 KParams make_kparams(const pog_params* p);

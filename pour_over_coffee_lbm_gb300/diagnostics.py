@@ -254,10 +254,10 @@ class SnapshotWriter:
             self._thread = None
 
 
-def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None) -> None:
+def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None, multiphase=None) -> None:
     """Everything a run needs to continue bit for bit: the raw distribution buffer in its
-    storage format, time index, flags, porosity, explicit force, LES velocity buffers, and the
-    particle, pour-nozzle and filter-paper state."""
+    storage format, time index, flags, porosity, explicit force, LES velocity buffers, the phase
+    indicator, and the particle, pour-nozzle, filter-paper and phase-field state."""
     s = solver
     d = {"t": np.int64(s.t), "step_count": np.int64(s.step_count), "storage": np.int32(s.cfg.storage),
          "shape": np.array([s.NX, s.NY, s.NZ], np.int64),
@@ -266,7 +266,8 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
          # rho/u as the last step left them (the moments the next coupling pass reads) and the
          # particle drag deposit of the last coupled step
          "rho": s._rho.cpu().numpy(), "u": s._u.cpu().numpy(), "macro_dirty": np.int8(s._macro_dirty),
-         "pdrag": s._pdrag.cpu().numpy(), "pdrag_active": np.int8(s._pdrag_active)}
+         "pdrag": s._pdrag.cpu().numpy(), "pdrag_active": np.int8(s._pdrag_active),
+         "phase": s._phase.cpu().numpy(), "rho_external": np.int8(s._rho_external)}
     if s._porosity is not None:
         d["porosity"] = s._porosity.cpu().numpy()
     if s._ul is not None:
@@ -280,6 +281,10 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
                   "p_since_sort": np.int64(-1 if p._since_sort is None else p._since_sort)})
     if pour is not None:
         d["pour"] = pour.block.cpu().numpy()
+    if multiphase is not None:
+        m = multiphase
+        d.update({"mp_phi": m.phi.cpu().numpy(), "mp_phi_new": m.phi_new.cpu().numpy(), "mp_mu": m.mu.cpu().numpy(),
+                  "mp_mu_live": np.int8(m._mu_live)})
     if filter_system is not None:
         d.update({"filter_accum": filter_system.accumulated_particles.cpu().numpy(),
                   "filter_blockage": filter_system.filter_blockage.cpu().numpy(),
@@ -289,7 +294,7 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     os.replace(tmp, path)
 
 
-def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None) -> None:
+def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None, multiphase=None) -> None:
     """Restore a save_checkpoint file into objects built with the same configuration."""
     s = solver
     z = np.load(path)
@@ -308,6 +313,9 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     s._u.copy_(torch.from_numpy(z["u"]))
     s._pdrag.copy_(torch.from_numpy(z["pdrag"]))
     s._pdrag_active = bool(z["pdrag_active"])
+    if "phase" in z:
+        s._phase.copy_(torch.from_numpy(z["phase"]))
+        s._rho_external = bool(z["rho_external"])
     s.t = int(z["t"])
     s.step_count = int(z["step_count"])
     s._macro_dirty = bool(z["macro_dirty"])
@@ -320,6 +328,13 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
         p._since_sort = None if ss < 0 else ss
     if pour is not None and "pour" in z:
         pour.block.copy_(torch.from_numpy(z["pour"]))
+    if multiphase is not None and "mp_phi" in z:
+        m = multiphase
+        m.phi.copy_(torch.from_numpy(z["mp_phi"]))
+        m.phi_new.copy_(torch.from_numpy(z["mp_phi_new"]))
+        m.mu.copy_(torch.from_numpy(z["mp_mu"]))
+        m._mu_live = bool(z["mp_mu_live"])
+        m.phi_changed()
     if filter_system is not None and "filter_accum" in z:
         filter_system.accumulated_particles.copy_(torch.from_numpy(z["filter_accum"]))
         filter_system.filter_blockage.copy_(torch.from_numpy(z["filter_blockage"]))

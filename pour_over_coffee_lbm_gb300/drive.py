@@ -75,22 +75,23 @@ class PressureGradientDrive:
     def apply_density_drive(self, rate_scale: float = 1.0, max_adjust: float = 0.001,
                             rho_min: float = 0.5, rho_max: float = 2.0) -> None:
         s = self.lbm
-        rho = s.rho.tensor  # current moments
+        rho = s._current_rho()
         _lib.check(self.lib.pog_density_drive(s._p, _lib.ptr(s._flags), _lib.ptr(rho), _lib.ptr(self._target),
                                               self.ADJUSTMENT_RATE * rate_scale, max_adjust, rho_min, rho_max,
                                               _lib.stream_handle()))
+        s._rho_external = True
 
     def compute_pressure_gradient(self) -> None:
         """pressure_force := capped -c_s^2 grad(rho) / rho on the non-solid cells."""
         s = self.lbm
         self.pressure_force.zero_()
-        _lib.check(self.lib.pog_pressure_force(s._p, _lib.ptr(s._flags), _lib.ptr(s.rho.tensor),
+        _lib.check(self.lib.pog_pressure_force(s._p, _lib.ptr(s._flags), _lib.ptr(s._current_rho()),
                                                _lib.ptr(self.pressure_force), 1.0, self.MAX_PRESSURE_FORCE,
                                                _lib.stream_handle()))
 
     def _accumulate(self, scale: float) -> None:
         s = self.lbm
-        _lib.check(self.lib.pog_pressure_force(s._p, _lib.ptr(s._flags), _lib.ptr(s.rho.tensor),
+        _lib.check(self.lib.pog_pressure_force(s._p, _lib.ptr(s._flags), _lib.ptr(s._current_rho()),
                                                _lib.ptr(s._force), scale, self.MAX_PRESSURE_FORCE,
                                                _lib.stream_handle()))
         s._force_written()

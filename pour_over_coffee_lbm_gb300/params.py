@@ -44,6 +44,7 @@ class PogParams(ctypes.Structure):
         ("inlet_control", ctypes.c_void_p),
         ("pour_control", ctypes.c_void_p),
         ("filter_blockage", ctypes.c_void_p),
+        ("phase", ctypes.c_void_p), ("tau_air", ctypes.c_float),
     ]
 
 
@@ -68,6 +69,7 @@ class LatticeConfig:
     forcing_mode: int = FORCING_GUO
     clamp_tau: bool = False
     tau: float = 0.8
+    tau_air: float = 0.8
     rho0: float = 1.0
     gravity: tuple = (0.0, 0.0, -1e-5)
     cs_smag: float = 0.1
@@ -100,7 +102,7 @@ class LatticeConfig:
         for f in ("nx", "ny", "nz", "storage", "les_mode", "drag_mode", "forcing_mode"):
             setattr(p, f, int(getattr(self, f)))
         p.clamp_tau = int(bool(self.clamp_tau))
-        for f in ("tau", "rho0", "cs_smag", "les_strain_floor", "les_nu_max", "tau_min",
+        for f in ("tau", "tau_air", "rho0", "cs_smag", "les_strain_floor", "les_nu_max", "tau_min",
                   "tau_max", "cone_apex_z", "cone_half_angle_deg", "cone_wall", "hole_radius",
                   "inlet_radius", "band_thickness", "center_x", "center_y", "porosity",
                   "permeability", "forchheimer", "drag_cap", "u_inlet", "rho_outlet"):

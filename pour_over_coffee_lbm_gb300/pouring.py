@@ -7,8 +7,8 @@ lives in a small device block (layout POG_POUR_* of include/pog.h) that the latt
 particle kernel read: the stream's downward force is applied inside the fused step to the cells
 of the nozzle's planes only, instead of through a separate body-force field, and
 pog_pour_advance moves the nozzle on the device (a captured CUDA graph replays a moving pour).
-The reference's phase-field update (apply_gradual_phase_change) belongs to the multiphase model,
-which this build does not include.
+apply_gradual_phase_change turns the stream's cells toward water in a MultiphaseFlow3D phase
+field (pog_pour_phase).
 """
 import math
 from typing import Optional
@@ -49,6 +49,7 @@ class PrecisePouringSystem:
         self._set(POUR_DIAMETER, self.POUR_DIAMETER_GRID)
         self._set(POUR_IMPACT_ZMIN, 0.3 * lattice.nz)
         self._solvers = []
+        self._dt = None
 
     def _set(self, idx: int, value: float) -> None:
         self.block[idx] = float(value)
@@ -79,9 +80,30 @@ class PrecisePouringSystem:
         lattice steps apply its force (apply_pouring_force, :132-160).  Call once per step."""
         if solver not in self._solvers:
             self._solvers.append(solver)
-        solver.set_pour_control(self.block)
-        self._set(POUR_DT, dt)
+        if solver._pour_ctl is not self.block:
+            solver.set_pour_control(self.block)
+        if self._dt != dt:  # a host write only when the step size changes (graph-capturable)
+            self._set(POUR_DT, dt)
+            self._dt = dt
         _lib.check(self.lib.pog_pour_advance(solver._p, _lib.stream_handle()))
+
+    def apply_gradual_phase_change(self, multiphase, solid=None, dt: float = 1.0) -> None:
+        """Turn the stream's cells toward water in a phase field (apply_gradual_phase_change,
+        :166-193): multiphase is a MultiphaseFlow3D (or its phi tensor, with the solver as
+        `solid`); non-solid cells of the stream change by clamp((1 - phi)/0.05, +-2) * intensity
+        * dt * flow_rate."""
+        if hasattr(multiphase, "phi_changed"):
+            phi, solver = multiphase.phi, multiphase.lbm
+        else:
+            phi, solver = multiphase, solid
+        if solver is None or not hasattr(solver, "_flags"):
+            raise ValueError("apply_gradual_phase_change needs the solver (for its solid cells)")
+        p = self.lattice.to_c()
+        p.pour_control = self.block.data_ptr()
+        _lib.check(self.lib.pog_pour_phase(p, _lib.ptr(solver._flags), _lib.ptr(phi), float(dt),
+                                           _lib.stream_handle()))
+        if hasattr(multiphase, "phi_changed"):
+            multiphase.phi_changed()
 
     def create_water_impact_force(self, particle_system=None, max_force: float = 1.0, dt: float = 1.0) -> None:
         """Let the stream push the particles near it in the next coupling passes

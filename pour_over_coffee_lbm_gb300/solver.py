@@ -164,6 +164,10 @@ class GB300LBMSolver:
         self._inlet_ctl = None
         self._pour_ctl = None
         self._blockage = None
+        # rho written by a plugin (phase density, density drive) until the next step; a lazy
+        # refresh of u then leaves it alone, as the reference's lbm.rho
+        self._rho_external = False
+        self._rho_scratch = None
         if porosity is not None:
             self.set_porosity(porosity)
         self.t = 0
@@ -187,11 +191,23 @@ class GB300LBMSolver:
     def _refresh_macro(self):
         if not self._macro_dirty:
             return
+        rho_out = self._rho
+        if self._rho_external:
+            if self._rho_scratch is None:
+                self._rho_scratch = torch.empty_like(self._rho)
+            rho_out = self._rho_scratch
         _lib.check(self.lib.pog_macroscopic(self._p, _lib.ptr(self._f), _lib.ptr(self._flags),
                                             self.t, _lib.ptr(self._force) if self._force_active else None,
                                             _lib.ptr(self._pdrag) if self._pdrag_active else None,
-                                            _lib.ptr(self._rho), _lib.ptr(self._u), self._s()))
+                                            _lib.ptr(rho_out), _lib.ptr(self._u), self._s()))
         self._macro_dirty = False
+
+    def _current_rho(self) -> torch.Tensor:
+        """The density field as the reference's lbm.rho holds it: a plugin-written density until
+        the next step, else the moments of the current state."""
+        if not self._rho_external:
+            self._refresh_macro()
+        return self._rho
 
     def _force_written(self):
         self._force_active = True
@@ -242,9 +258,12 @@ class GB300LBMSolver:
 
     @property
     def phase(self) -> FieldView:
-        """Single phase: phi = 1 everywhere (the LES phase gate of les_turbulence.py:364
-        passes)."""
-        return FieldView(self._phase)
+        """Phase indicator (0 air, 1 water).  1 everywhere for single-phase runs; the step reads
+        it once a phase field is attached (set_phase_field, MultiphaseFlow3D)."""
+        return FieldView(self._phase, on_write=self._phase_written)
+
+    def _phase_written(self):
+        self._macro_dirty = True
 
     @property
     def body_force(self) -> FieldView:
@@ -353,6 +372,7 @@ class GB300LBMSolver:
         # that step started from, as the reference's solver.rho/u after step()); otherwise they
         # are recomputed from the current state when read.
         self._macro_dirty = not want_macro
+        self._rho_external = False
         return self._red if reduce else None
 
     def step(self) -> None:
@@ -429,15 +449,15 @@ class GB300LBMSolver:
         self._inlet_ctl = control
         self._p.inlet_control = None if control is None else control.data_ptr()
 
-    def save_checkpoint(self, path: str, particles=None, pour=None, filter_system=None) -> None:
-        """Raw state of the run (and of its particles / pour nozzle / filter paper) to an .npz
-        file that load_checkpoint continues bit for bit."""
+    def save_checkpoint(self, path: str, particles=None, pour=None, filter_system=None, multiphase=None) -> None:
+        """Raw state of the run (and of its particles / pour nozzle / filter paper / phase field)
+        to an .npz file that load_checkpoint continues bit for bit."""
         from .diagnostics import save_checkpoint
-        save_checkpoint(path, self, particles, pour, filter_system)
+        save_checkpoint(path, self, particles, pour, filter_system, multiphase)
 
-    def load_checkpoint(self, path: str, particles=None, pour=None, filter_system=None) -> None:
+    def load_checkpoint(self, path: str, particles=None, pour=None, filter_system=None, multiphase=None) -> None:
         from .diagnostics import load_checkpoint
-        load_checkpoint(path, self, particles, pour, filter_system)
+        load_checkpoint(path, self, particles, pour, filter_system, multiphase)
 
     def set_pour_control(self, block: Optional[torch.Tensor]) -> None:
         """Attach a pour-nozzle block (PrecisePouringSystem.block: CUDA float32, POG_POUR_NFIELDS
@@ -447,6 +467,21 @@ class GB300LBMSolver:
                 raise ValueError("pour block must be a contiguous CUDA float32 tensor of 20 values")
         self._pour_ctl = block
         self._p.pour_control = None if block is None else block.data_ptr()
+        self._macro_dirty = True
+
+    def set_phase_field(self, phase: Optional[torch.Tensor], tau_air: Optional[float] = None) -> None:
+        """Let the step read a phase indicator (CUDA float32, one value per cell, 0 air .. 1 water):
+        gravity on the water fraction, tau = tau where phase > 0.5 else tau_air, no LES where
+        |phase| < 0.9.  None returns to single-phase water."""
+        if phase is not None:
+            if (phase.dtype != torch.float32 or phase.numel() != self.n or not phase.is_cuda
+                    or not phase.is_contiguous()):
+                raise ValueError("phase must be a contiguous CUDA float32 tensor of ncell values")
+        if tau_air is not None:
+            self._p.tau_air = float(tau_air)
+        self._phase_attached = phase
+        self._p.phase = None if phase is None else phase.data_ptr()
+        _lib.check(self.lib.pog_validate_params(self._p))
         self._macro_dirty = True
 
     def set_filter_blockage(self, blockage: Optional[torch.Tensor]) -> None:
@@ -597,6 +632,7 @@ class StepGraph:
         s.t += self.nsteps
         s.step_count += self.nsteps
         s._macro_dirty = self.ps is None
+        s._rho_external = False
         if self.ps is not None:
             self.ps._since_sort = self._ps_after
 
