@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--error-steps", type=int, default=2000, help="steps of the FP64 error runs")
     ap.add_argument("--small", action="store_true", help="64^3 / 2,000 particles (profiling)")
+    ap.add_argument("--scale-steps", type=int, default=5000,
+                    help="coupled steps of the 320x320x384 / 1M-particle line (0 = skip)")
     ap.add_argument("--precision-only", choices=["fp32", "fp16s", "bf16s"], default=None,
                     help="time only the 256^3 precision case in this storage for --steps steps (profiling)")
     ap.add_argument("--precision-case", choices=["les_band", "plain"], default="les_band")
@@ -309,6 +311,136 @@ def plugin_rows(cfg, pc, steps, peak):
     return out
 
 
+def differentiation_rows(peak):
+    """96^3 + band with per-cell porosity 0.6 +- 0.05 and the 16-coefficient inlet profile: 500
+    steps forward and the adjoint with checkpoints every 50, FP32 and FP64, timed; FP64 central
+    differences (h = 1e-3) on the 8 porous cells with the largest gradients and all 16
+    coefficients.  The particles of the case are not part of the differentiated step."""
+    import numpy as np
+    import torch
+    from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint
+    from pour_over_coffee_lbm_gb300.params import (CELL_POROUS, STORE_F32, STORE_F64, differentiation_96,
+                                                   porosity_field)
+    cfg, _ = differentiation_96()
+    T, K = 500, 50
+    out = {"workload": "%dx%dx%d D3Q19 + LES(local) + band, porosity 0.6 +- 0.05, 16-coefficient inlet; "
+                       "J = sum of outflow over %d steps, checkpoints every %d" % (cfg.nx, cfg.ny, cfg.nz, T, K)}
+    res = {}
+    for name, st in (("fp32", STORE_F32), ("fp64", STORE_F64)):
+        c = cfg.replace(storage=st)
+        run = OutflowAdjoint(c, T, K)
+        fl = run.flags.cpu().numpy()
+        eps = torch.as_tensor(porosity_field(c, fl, seed=1234)).reshape(c.nz, c.ny, c.nx).cuda()
+        run.forward(eps, c.inlet_coef)  # warm-up
+        run.backward()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        J = run.forward(eps, c.inlet_coef)
+        ev[1].record()
+        r = run.backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        fwd, bwd = ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3
+        out[name] = {"forward_ms": round(fwd * 1e3, 2), "backward_ms": round(bwd * 1e3, 2),
+                     "adjoint_mlups": round(c.ncell * T / bwd / 1e6, 1), "loss": J}
+        res[name] = (run, eps, fl, r)
+    g32, g64 = res["fp32"][3], res["fp64"][3]
+    out["fp32_vs_fp64_grad_rel"] = {
+        "inlet": float((g32.grad_inlet - g64.grad_inlet).norm() / g64.grad_inlet.norm()),
+        "porosity": float((g32.grad_porosity - g64.grad_porosity).norm() / g64.grad_porosity.norm())}
+    run, eps, fl, r = res["fp64"]
+    h = 1e-3
+    coef = np.array(cfg.inlet_coef, np.float64)
+    fds, ads = [], []
+    for k in range(16):
+        cp, cm = coef.copy(), coef.copy()
+        cp[k] += h
+        cm[k] -= h
+        fds.append((run.loss(eps, cp) - run.loss(eps, cm)) / (2 * h))
+        ads.append(r.grad_inlet[k].item())
+    fds, ads = np.array(fds), np.array(ads)
+    err_in = float(np.max(np.abs(ads - fds) / np.maximum(np.abs(fds), 1e-30)))
+    err_in_norm = float(np.max(np.abs(ads - fds)) / np.max(np.abs(fds)))
+    ge = r.grad_porosity.cpu().numpy().reshape(-1)
+    band = np.flatnonzero((fl.reshape(-1) & CELL_POROUS) != 0)
+    flat = eps.reshape(-1)
+    err_eps = 0.0
+    for c in band[np.argsort(-np.abs(ge[band]))[:8]]:
+        ep, em = flat.clone(), flat.clone()
+        ep[c] += h
+        em[c] -= h
+        hh = (ep[c].double() - em[c].double()).item() / 2
+        fd = (run.loss(ep.reshape(eps.shape), coef) - run.loss(em.reshape(eps.shape), coef)) / (2 * hh)
+        err_eps = max(err_eps, abs(ge[c] - fd) / max(abs(fd), 1e-30))
+    out["fd_max_rel_err_fp64"] = {"inlet_16": err_in, "inlet_16_vs_largest": err_in_norm, "porosity_8": err_eps,
+                                  "h": h, "inlet_fd": fds.tolist(), "inlet_adjoint": ads.tolist()}
+    del res, run
+    torch.cuda.empty_cache()
+    return out
+
+
+def scale_row(steps, adj_steps=200, ckpt=20):
+    """320x320x384 FP16S + LES + band + 1,000,000 particles: `steps` two-way coupled steps
+    (graph-replayed), then the outflow adjoint over the last adj_steps (recomputed in FP32 from the
+    FP16S state, checkpoints every ckpt)."""
+    import torch
+    from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint
+    from pour_over_coffee_lbm_gb300.params import STORE_F32, scale_320x384
+    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    cfg, pc = scale_320x384()
+    s = GB300LBMSolver(cfg)
+    ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
+    ps.seed()
+    for _ in range(4):
+        s.step_with_two_way_coupling(ps)
+    g = s.capture(GRAPH_STEPS, ps)
+    g.replay()
+    torch.cuda.synchronize()
+    n_fwd = max(GRAPH_STEPS, ((steps - adj_steps - 4 - GRAPH_STEPS) // GRAPH_STEPS) * GRAPH_STEPS)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(n_fwd // GRAPH_STEPS):
+        g.replay()
+    ev1.record()
+    torch.cuda.synchronize()
+    el = ev0.elapsed_time(ev1) / 1e3
+    stable = bool(s.check_stability())
+    del g
+    nat = torch.empty((19, cfg.nz, cfg.ny, cfg.nx), dtype=torch.float32, device="cuda")
+    from pour_over_coffee_lbm_gb300 import _lib
+    _lib.check(s.lib.pog_export_natural(s._p, _lib.ptr(s._f), _lib.ptr(s._flags), s.t, _lib.ptr(nat), STORE_F32,
+                                        _lib.stream_handle()))
+    done = s.t
+    del s, ps
+    torch.cuda.empty_cache()
+    run = OutflowAdjoint(cfg.replace(storage=STORE_F32), adj_steps, ckpt)
+    # gradients w.r.t. the band's per-cell porosity (the inlet is more than adj_steps planes
+    # above the outlet, so its coefficients cannot reach J within the window)
+    eps = torch.full((cfg.nz, cfg.ny, cfg.nx), cfg.porosity, dtype=torch.float32, device="cuda")
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    J = run.forward(eps, cfg.inlet_coef, initial=nat)
+    e[1].record()
+    r = run.backward(want_porosity_grad=True)
+    e[2].record()
+    torch.cuda.synchronize()
+    fwd, bwd = e[0].elapsed_time(e[1]) / 1e3, e[1].elapsed_time(e[2]) / 1e3
+    out = {"workload": "%dx%dx%d FP16S + LES(local) + band + %d particles, two-way coupled; adjoint of the outflow "
+                       "over the last %d steps (FP32 recompute, checkpoints every %d)"
+                       % (cfg.nx, cfg.ny, cfg.nz, pc.count, adj_steps, ckpt),
+           "coupled_steps": done, "coupled_mlups": round(cfg.ncell * n_fwd / el / 1e6, 1),
+           "coupled_ms_per_step": round(el * 1e3 / n_fwd, 4), "stable": stable,
+           "adjoint": {"steps": adj_steps, "forward_ms": round(fwd * 1e3, 1), "backward_ms": round(bwd * 1e3, 1),
+                       "adjoint_mlups": round(cfg.ncell * adj_steps / bwd / 1e6, 1), "loss": J,
+                       "grad_porosity_finite": bool(torch.isfinite(r.grad_porosity).all()),
+                       "grad_porosity_nonzero_cells": int((r.grad_porosity != 0).sum().item())},
+           "max_memory_gb": round(torch.cuda.max_memory_allocated() / 1e9, 1)}
+    del run, nat, eps, r
+    torch.cuda.empty_cache()
+    return out
+
+
 PRECISION_CASES = {
     # the 256^3 target case: D3Q19 + LES (local strain) + 3-cell porous band
     "les_band": {},
@@ -531,9 +663,12 @@ def run_ours(args):
                            "fp16s_vs_fp32_mlups": round(p16["mlups"] / p32["mlups"], 3),
                            "bf16s_vs_fp32_mlups": round(pb16["mlups"] / p32["mlups"], 3)}
 
-    rows = None
+    rows = diff = scale = None
     if not args.no_extra and not args.small and rank == 0:
         rows = plugin_rows(cfg, pc, 200, peak)
+        diff = differentiation_rows(peak)
+        if args.scale_steps > 0:
+            scale = scale_row(args.scale_steps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -565,6 +700,8 @@ def run_ours(args):
             "clocks": clk,
             "precision_256": extra,
             "plugin_rows": rows,
+            "differentiation_96": diff,
+            "scale_320x320x384": scale,
             "diagnostics": {"mass": diag["mass"], "max_velocity": diag["max_velocity"], "stable": diag["stable"]},
         }
         print(json.dumps(line), flush=True)

@@ -64,15 +64,25 @@ class OutflowAdjoint:
                                           None, None, _lib.ptr(self._eps), None, None, None,
                                           _lib.ptr(red), _lib.stream_handle()))
 
-    def forward(self, porosity: Optional[torch.Tensor], inlet_coef) -> float:
-        """Run the forward pass, keep checkpoints, return J."""
+    def forward(self, porosity: Optional[torch.Tensor], inlet_coef, initial: Optional[torch.Tensor] = None) -> float:
+        """Run the forward pass, keep checkpoints, return J.  initial: plain distributions f_q in
+        natural layout [19, NZ, NY, NX], float32 or float64 on the device (pog_export_natural's
+        output), the T steps start from (default: equilibrium at rest)."""
         self._p = self._params(inlet_coef)
         self._eps = None if porosity is None else porosity.to(self.device, torch.float32).contiguous().reshape(self.shape)
         s = _lib.stream_handle()
         cur = self._states[0]
         nxt = self._states[1] if self.K > 1 else torch.empty_like(cur)
-        _lib.check(self.lib.pog_init_equilibrium(self._p, _lib.ptr(cur), _lib.ptr(self.flags),
-                                                 float(self.cfg.rho0), 0.0, 0.0, 0.0, s))
+        if initial is None:
+            _lib.check(self.lib.pog_init_equilibrium(self._p, _lib.ptr(cur), _lib.ptr(self.flags),
+                                                     float(self.cfg.rho0), 0.0, 0.0, 0.0, s))
+        else:
+            if initial.dtype not in (torch.float32, torch.float64) or initial.numel() != cur.numel():
+                raise ValueError("initial must be float32/float64 [19, NZ, NY, NX]")
+            src = initial.contiguous()
+            in_store = STORE_F32 if src.dtype == torch.float32 else STORE_F64
+            _lib.check(self.lib.pog_import_natural(self._p, _lib.ptr(src), in_store, _lib.ptr(self.flags),
+                                                   _lib.ptr(cur), s))
         self._red.zero_()
         for t in range(self.T):
             if t % self.K == 0:

@@ -24,9 +24,24 @@ static PhaseGrid phase_grid(const pog_params* p) {
   return g;
 }
 
-__device__ __forceinline__ bool phase_interior(const PhaseGrid& g, uint32_t c) {
-  const uint32_t i = c % g.nx, j = (c / g.nx) % g.ny, k = c / g.plane;
-  return i >= 1 && i + 1 < g.nx && j >= 1 && j + 1 < g.ny && k >= 1 && k + 1 < g.nz;
+// One thread per cell on a (x, y, z) grid of PHASE_BX x PHASE_BY blocks, one plane per grid z:
+// the cell indices come without divisions and a warp covers 32 consecutive x.
+constexpr int PHASE_BX = 64, PHASE_BY = 4;
+
+struct PhaseCell {
+  uint32_t i, j, k, c;
+  bool valid, interior;
+};
+
+__device__ __forceinline__ PhaseCell phase_cell(const PhaseGrid& g) {
+  PhaseCell p;
+  p.i = blockIdx.x * PHASE_BX + threadIdx.x;
+  p.j = blockIdx.y * PHASE_BY + threadIdx.y;
+  p.k = blockIdx.z;
+  p.valid = p.i < g.nx && p.j < g.ny;
+  p.c = (p.k * g.ny + p.j) * g.nx + p.i;
+  p.interior = p.valid && p.i >= 1 && p.i + 1 < g.nx && p.j >= 1 && p.j + 1 < g.ny && p.k >= 1 && p.k + 1 < g.nz;
+  return p;
 }
 
 // 6-neighbour sum minus 6 x centre, in the reference's order (x+, x-, y+, y-, z+, z-)
@@ -36,34 +51,34 @@ __device__ __forceinline__ float lap7(const float* __restrict__ a, const PhaseGr
 
 // compute_chemical_potential (:80-109): mu = phi^3 - phi - kappa lap(phi)
 __global__ void phase_mu_kernel(PhaseGrid g, const float* __restrict__ phi, float kappa, float* __restrict__ mu) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < g.n; c += gridDim.x * blockDim.x) {
-    if (!phase_interior(g, c)) continue;
-    const float p = phi[c];
-    const float lap = lap7(phi, g, c);
-    mu[c] = (p * p * p - p) + (-kappa * lap);
-  }
+  const PhaseCell pc_ = phase_cell(g);
+  if (!pc_.interior) return;
+  const uint32_t c = pc_.c;
+  const float p = phi[c];
+  const float lap = lap7(phi, g, c);
+  mu[c] = (p * p * p - p) + (-kappa * lap);
 }
 
 // compute_gradients (:111-132): grad phi by central differences, unit normal where |grad| > 1e-10
 __global__ void phase_normals_kernel(PhaseGrid g, const float* __restrict__ phi, float* __restrict__ normal,
                                      float* __restrict__ gmag) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < g.n; c += gridDim.x * blockDim.x) {
-    if (!phase_interior(g, c)) continue;
-    const float gx = (phi[c + 1] - phi[c - 1]) * 0.5f;
-    const float gy = (phi[c + g.nx] - phi[c - g.nx]) * 0.5f;
-    const float gz = (phi[c + g.plane] - phi[c - g.plane]) * 0.5f;
-    const float m = sqrtf(gx * gx + gy * gy + gz * gz);
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-    if (m > 1e-10f) {
-      nx = gx / m;
-      ny = gy / m;
-      nz = gz / m;
-    }
-    normal[c] = nx;
-    normal[g.n + c] = ny;
-    normal[2 * g.n + c] = nz;
-    gmag[c] = m;
+  const PhaseCell pc_ = phase_cell(g);
+  if (!pc_.interior) return;
+  const uint32_t c = pc_.c;
+  const float gx = (phi[c + 1] - phi[c - 1]) * 0.5f;
+  const float gy = (phi[c + g.nx] - phi[c - g.nx]) * 0.5f;
+  const float gz = (phi[c + g.plane] - phi[c - g.plane]) * 0.5f;
+  const float m = sqrtf(gx * gx + gy * gy + gz * gz);
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+  if (m > 1e-10f) {
+    nx = gx / m;
+    ny = gy / m;
+    nz = gz / m;
   }
+  normal[c] = nx;
+  normal[g.n + c] = ny;
+  normal[2 * g.n + c] = nz;
+  gmag[c] = m;
 }
 
 // compute_curvature (:134-149), compute_surface_tension_force (:313-331) and
@@ -76,40 +91,40 @@ __global__ void phase_tension_kernel(PhaseGrid g, const uint32_t* __restrict__ f
                                      const float* __restrict__ normal, const float* __restrict__ gmag,
                                      const float* __restrict__ rho, float sigma, float* __restrict__ body_force,
                                      float* __restrict__ curvature, float* __restrict__ sforce) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < g.n; c += gridDim.x * blockDim.x) {
-    if (!phase_interior(g, c)) continue;
-    const float m = gmag[c];
-    float kap = 0.0f, fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    bool on = false;
-    if (m > 1e-10f) {
-      on = fabsf(phi[c]) < 0.9f;
-      if (on || curvature) {
-        const float* nx = normal;
-        const float* ny = normal + g.n;
-        const float* nz = normal + 2 * g.n;
-        kap = (nx[c + 1] - nx[c - 1]) * 0.5f + (ny[c + g.nx] - ny[c - g.nx]) * 0.5f +
-              (nz[c + g.plane] - nz[c - g.plane]) * 0.5f;
-      }
-      if (on) {
-        const float fm = sigma * kap * m;
-        fx = fm * normal[c];
-        fy = fm * normal[g.n + c];
-        fz = fm * normal[2 * g.n + c];
-      }
+  const PhaseCell pc_ = phase_cell(g);
+  if (!pc_.interior) return;
+  const uint32_t c = pc_.c;
+  const float m = gmag[c];
+  float kap = 0.0f, fx = 0.0f, fy = 0.0f, fz = 0.0f;
+  bool on = false;
+  if (m > 1e-10f) {
+    on = fabsf(phi[c]) < 0.9f;
+    if (on || curvature) {
+      const float* nx = normal;
+      const float* ny = normal + g.n;
+      const float* nz = normal + 2 * g.n;
+      kap = (nx[c + 1] - nx[c - 1]) * 0.5f + (ny[c + g.nx] - ny[c - g.nx]) * 0.5f +
+            (nz[c + g.plane] - nz[c - g.plane]) * 0.5f;
     }
-    if (curvature) curvature[c] = kap;
-    if (sforce) {
-      sforce[c] = fx;
-      sforce[g.n + c] = fy;
-      sforce[2 * g.n + c] = fz;
+    if (on) {
+      const float fm = sigma * kap * m;
+      fx = fm * normal[c];
+      fy = fm * normal[g.n + c];
+      fz = fm * normal[2 * g.n + c];
     }
-    if (on && body_force && !(flags[c] & POG_CELL_SOLID)) {
-      const float r = rho[c];
-      if (r > 1e-10f) {
-        body_force[c] += fx / r;
-        body_force[g.n + c] += fy / r;
-        body_force[2 * g.n + c] += fz / r;
-      }
+  }
+  if (curvature) curvature[c] = kap;
+  if (sforce) {
+    sforce[c] = fx;
+    sforce[g.n + c] = fy;
+    sforce[2 * g.n + c] = fz;
+  }
+  if (on && body_force && !(flags[c] & POG_CELL_SOLID)) {
+    const float r = rho[c];
+    if (r > 1e-10f) {
+      body_force[c] += fx / r;
+      body_force[g.n + c] += fy / r;
+      body_force[2 * g.n + c] += fz / r;
     }
   }
 }
@@ -123,47 +138,49 @@ __global__ void phase_update_kernel(PhaseGrid g, const uint32_t* __restrict__ fl
                                     float* __restrict__ phi_new, const float* __restrict__ u,
                                     const float* __restrict__ mu, float mobility, float dt, float rho_air,
                                     float drho, float* __restrict__ rho_out, float* __restrict__ phase_out) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < g.n; c += gridDim.x * blockDim.x) {
-    const float p = phi[c];
-    float pn = p;
-    if (phase_interior(g, c)) {
-      float ux = 0.0f, uy = 0.0f, uz = 0.0f;
-      if (!(flags[c] & POG_CELL_SOLID)) {
-        ux = u[c];
-        uy = u[g.n + c];
-        uz = u[2 * g.n + c];
-      }
-      const float dx = ux > 0.0f ? p - phi[c - 1] : phi[c + 1] - p;
-      const float dy = uy > 0.0f ? p - phi[c - g.nx] : phi[c + g.nx] - p;
-      const float dz = uz > 0.0f ? p - phi[c - g.plane] : phi[c + g.plane] - p;
-      const float conv = -(ux * dx + uy * dy + uz * dz);
-      float diff = 0.0f;
-      if (mu) diff = mobility * lap7(mu, g, c);
-      pn = p + dt * (conv + diff);
-      pn = fmaxf(-1.0f, fminf(1.0f, pn));
-      if (fabsf(p) < 0.99f) {
-        const float lap = lap7(phi, g, c);
-        const float chem = p * (p * p - 1.0f) - 0.01f * lap;
-        pn = pn + -0.001f * chem * dt;
-      }
+  const PhaseCell pc_ = phase_cell(g);
+  if (!pc_.valid) return;
+  const uint32_t c = pc_.c;
+  const float p = phi[c];
+  float pn = p;
+  if (pc_.interior) {
+    float ux = 0.0f, uy = 0.0f, uz = 0.0f;
+    if (!(flags[c] & POG_CELL_SOLID)) {
+      ux = u[c];
+      uy = u[g.n + c];
+      uz = u[2 * g.n + c];
     }
-    phi_new[c] = pn;
-    if (rho_out) {
-      const float pc = fmaxf(-1.0f, fminf(1.0f, pn));
-      rho_out[c] = rho_air + drho * (pc + 1.0f) / 2.0f;
-      phase_out[c] = (pc + 1.0f) / 2.0f;
+    const float dx = ux > 0.0f ? p - phi[c - 1] : phi[c + 1] - p;
+    const float dy = uy > 0.0f ? p - phi[c - g.nx] : phi[c + g.nx] - p;
+    const float dz = uz > 0.0f ? p - phi[c - g.plane] : phi[c + g.plane] - p;
+    const float conv = -(ux * dx + uy * dy + uz * dz);
+    float diff = 0.0f;
+    if (mu) diff = mobility * lap7(mu, g, c);
+    pn = p + dt * (conv + diff);
+    pn = fmaxf(-1.0f, fminf(1.0f, pn));
+    if (fabsf(p) < 0.99f) {
+      const float lap = lap7(phi, g, c);
+      const float chem = p * (p * p - 1.0f) - 0.01f * lap;
+      pn = pn + -0.001f * chem * dt;
     }
+  }
+  phi_new[c] = pn;
+  if (rho_out) {
+    const float pc = fmaxf(-1.0f, fminf(1.0f, pn));
+    rho_out[c] = rho_air + drho * (pc + 1.0f) / 2.0f;
+    phase_out[c] = (pc + 1.0f) / 2.0f;
   }
 }
 
 // update_density_from_phase (:365-381) alone
 __global__ void phase_properties_kernel(PhaseGrid g, const float* __restrict__ phi, float rho_air, float drho,
                                         float* __restrict__ rho_out, float* __restrict__ phase_out) {
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < g.n; c += gridDim.x * blockDim.x) {
-    const float pc = fmaxf(-1.0f, fminf(1.0f, phi[c]));
-    rho_out[c] = rho_air + drho * (pc + 1.0f) / 2.0f;
-    phase_out[c] = (pc + 1.0f) / 2.0f;
-  }
+  const PhaseCell pc_ = phase_cell(g);
+  if (!pc_.valid) return;
+  const uint32_t c = pc_.c;
+  const float pc = fmaxf(-1.0f, fminf(1.0f, phi[c]));
+  rho_out[c] = rho_air + drho * (pc + 1.0f) / 2.0f;
+  phase_out[c] = (pc + 1.0f) / 2.0f;
 }
 
 // apply_gradual_phase_change (precise_pouring.py:166-193): non-solid cells of the stream move
@@ -199,6 +216,10 @@ static int phase_blocks(uint32_t n) {
   const long long want = ((long long)n + 255) / 256;
   return (int)(want < 152 * 16 ? want : 152 * 16);
 }
+static dim3 phase_grid3(const PhaseGrid& g) {
+  return dim3((g.nx + PHASE_BX - 1) / PHASE_BX, (g.ny + PHASE_BY - 1) / PHASE_BY, g.nz);
+}
+static const dim3 kPhaseBlock(PHASE_BX, PHASE_BY, 1);
 
 }  // namespace pog
 
@@ -211,7 +232,7 @@ int pog_phase_chemical_potential(const pog_params* p, const float* phi, float ka
   if (rc) return rc;
   if (!phi || !mu) return set_error(POG_E_ARG, "NULL pointer");
   const PhaseGrid g = phase_grid(p);
-  phase_mu_kernel<<<phase_blocks(g.n), 256, 0, (cudaStream_t)stream>>>(g, phi, kappa, mu);
+  phase_mu_kernel<<<phase_grid3(g), kPhaseBlock, 0, (cudaStream_t)stream>>>(g, phi, kappa, mu);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;
@@ -222,7 +243,7 @@ int pog_phase_normals(const pog_params* p, const float* phi, float* normal, floa
   if (rc) return rc;
   if (!phi || !normal || !gmag) return set_error(POG_E_ARG, "NULL pointer");
   const PhaseGrid g = phase_grid(p);
-  phase_normals_kernel<<<phase_blocks(g.n), 256, 0, (cudaStream_t)stream>>>(g, phi, normal, gmag);
+  phase_normals_kernel<<<phase_grid3(g), kPhaseBlock, 0, (cudaStream_t)stream>>>(g, phi, normal, gmag);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;
@@ -236,7 +257,7 @@ int pog_phase_surface_tension(const pog_params* p, const uint32_t* flags, const 
   if (!flags || !phi || !normal || !gmag) return set_error(POG_E_ARG, "NULL pointer");
   if (body_force && !rho) return set_error(POG_E_ARG, "body_force needs rho");
   const PhaseGrid g = phase_grid(p);
-  phase_tension_kernel<<<phase_blocks(g.n), 256, 0, (cudaStream_t)stream>>>(g, flags, phi, normal, gmag, rho, sigma,
+  phase_tension_kernel<<<phase_grid3(g), kPhaseBlock, 0, (cudaStream_t)stream>>>(g, flags, phi, normal, gmag, rho, sigma,
                                                                             body_force, curvature, surface_force);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
@@ -252,7 +273,7 @@ int pog_phase_update(const pog_params* p, const uint32_t* flags, const float* ph
   if (phi == phi_new) return set_error(POG_E_ARG, "phi and phi_new must differ");
   if (!rho != !phase) return set_error(POG_E_ARG, "rho and phase go together");
   const PhaseGrid g = phase_grid(p);
-  phase_update_kernel<<<phase_blocks(g.n), 256, 0, (cudaStream_t)stream>>>(
+  phase_update_kernel<<<phase_grid3(g), kPhaseBlock, 0, (cudaStream_t)stream>>>(
       g, flags, phi, phi_new, u, mu, mobility, dt, rho_air, (float)((double)rho_water - (double)rho_air), rho, phase);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
@@ -265,7 +286,7 @@ int pog_phase_properties(const pog_params* p, const float* phi, float rho_air, f
   if (rc) return rc;
   if (!phi || !rho || !phase) return set_error(POG_E_ARG, "NULL pointer");
   const PhaseGrid g = phase_grid(p);
-  phase_properties_kernel<<<phase_blocks(g.n), 256, 0, (cudaStream_t)stream>>>(
+  phase_properties_kernel<<<phase_grid3(g), kPhaseBlock, 0, (cudaStream_t)stream>>>(
       g, phi, rho_air, (float)((double)rho_water - (double)rho_air), rho, phase);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());

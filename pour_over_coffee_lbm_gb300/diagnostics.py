@@ -281,6 +281,7 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
                   "p_since_sort": np.int64(-1 if p._since_sort is None else p._since_sort)})
     if pour is not None:
         d["pour"] = pour.block.cpu().numpy()
+        d["pour_attached"] = np.int8(s._pour_ctl is pour.block)
     if multiphase is not None:
         m = multiphase
         d.update({"mp_phi": m.phi.cpu().numpy(), "mp_phi_new": m.phi_new.cpu().numpy(), "mp_mu": m.mu.cpu().numpy(),
@@ -316,6 +317,10 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     if "phase" in z:
         s._phase.copy_(torch.from_numpy(z["phase"]))
         s._rho_external = bool(z["rho_external"])
+    if pour is not None and "pour" in z:
+        pour.block.copy_(torch.from_numpy(z["pour"]))
+        if "pour_attached" in z and bool(z["pour_attached"]):
+            s.set_pour_control(pour.block)  # before the moments' state is restored below
     s.t = int(z["t"])
     s.step_count = int(z["step_count"])
     s._macro_dirty = bool(z["macro_dirty"])
@@ -326,8 +331,6 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
             getattr(p, "_" + name).copy_(torch.from_numpy(z["p_" + name]))
         ss = int(z["p_since_sort"])
         p._since_sort = None if ss < 0 else ss
-    if pour is not None and "pour" in z:
-        pour.block.copy_(torch.from_numpy(z["pour"]))
     if multiphase is not None and "mp_phi" in z:
         m = multiphase
         m.phi.copy_(torch.from_numpy(z["mp_phi"]))

@@ -119,3 +119,25 @@ def test_adjoint_rejects_unsupported_modes(cuda):
     with pytest.raises(_lib.PogError):
         run.forward(None, cfg.inlet_coef)
         run.backward()
+
+
+def test_forward_from_a_given_state(cuda):
+    """J over steps 6..13 from the exported state at t = 6 equals J(14) - J(6) from rest."""
+    from pour_over_coffee_lbm_gb300 import _lib
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    cfg = _case().replace(storage=STORE_F64, nx=16, ny=16, nz=16)
+    j14 = OutflowAdjoint(cfg, steps=14, checkpoint_every=7).forward(None, cfg.inlet_coef)
+    j6 = OutflowAdjoint(cfg, steps=6, checkpoint_every=3).forward(None, cfg.inlet_coef)
+    s = GB300LBMSolver(cfg)
+    s.run(6)
+    nat = torch.empty((19, cfg.nz, cfg.ny, cfg.nx), dtype=torch.float64, device="cuda")
+    _lib.check(s.lib.pog_export_natural(s._p, _lib.ptr(s._f), _lib.ptr(s._flags), s.t, _lib.ptr(nat), STORE_F64,
+                                        _lib.stream_handle()))
+    run = OutflowAdjoint(cfg, steps=8, checkpoint_every=4)
+    j8 = run.forward(None, cfg.inlet_coef, initial=nat)
+    assert abs(j8 - (j14 - j6)) <= 1e-9 * abs(j14)
+    # the band next to the outlet is within reach of 8 steps (the inlet, 13 planes up, is not)
+    eps = torch.full((cfg.nz, cfg.ny, cfg.nx), cfg.porosity, dtype=torch.float32, device="cuda")
+    run.forward(eps, cfg.inlet_coef, initial=nat)
+    r = run.backward()
+    assert torch.isfinite(r.grad_porosity).all() and r.grad_porosity.abs().max() > 0
