@@ -190,6 +190,10 @@ typedef struct pog_particle_params {
   float wall_pullback;  /* radius a violating particle is moved to, fraction (0.8)             */
   float wall_damping;   /* velocity factor on a wall hit (0.3)                                 */
   float z_floor;        /* particles are kept above cone_apex_z + z_floor                      */
+  /* Optional DEVICE array [np] or NULL: pog_particles_couple writes the base cell (i, j, k
+   * corner) of each particle's 8-cell drag deposit, -1 for a particle that deposited nothing, so
+   * that pog_particles_clear_deposit can zero exactly those cells after the lattice step. */
+  int32_t* deposit_cells;
 } pog_particle_params;
 
 /* ---- library ------------------------------------------------------------------------------- */
@@ -398,6 +402,13 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
                          float* vel, const float* diameter, float* drag_old, int32_t* active,
                          int np, const int32_t* order, const float* u, float* pdrag,
                          long long* pdrag_fix, float* u_at_particle, void* stream);
+/* Zero the 4 x 8 deposit slots pdrag[a][corner + {0,1} + nx {0,1} + nx ny {0,1}] of every
+ * particle whose deposit_cells entry (from pog_particles_couple) is >= 0: after the lattice step
+ * has read the deposit, this returns pdrag to all zeros at the cost of the particles' cells
+ * instead of a full-field fill.  order (nullable): the coupling pass's particle order, so that
+ * neighbouring threads write neighbouring cells. */
+int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cells, int np,
+                                const int32_t* order, float* pdrag, void* stream);
 /* pdrag[a][c] = pdrag_fix[a][c] * 2^-32, a = 0..3 (deterministic-mode conversion). */
 int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* pdrag,
                         void* stream);

@@ -187,6 +187,7 @@ struct PKParams {
   float zlo, zhi, margin, pullback, damping;
   int drag_model, deterministic;
   const float* pour;  // device pour-nozzle block or null
+  int32_t* dep_cells;  // device [np]: base cell of each particle's deposit (-1: none) or null
 };
 
 // Impact force of the pour stream on a particle at (x, y, z) (create_water_impact_force,
@@ -372,6 +373,7 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
         dep_ok = true;
       }
     }
+    if (P.dep_cells && q >= 0) P.dep_cells[q] = dep_ok ? (int32_t)c0 : -1;
     // Deposit the drag coefficient and its momentum weight (Kp += w beta, Kv += w beta v_new)
     // with the gather weights at the pre-update position; the lattice step applies the
     // particle force on the fluid, Kv - Kp u, implicitly in u.
@@ -391,6 +393,23 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
       }
     }
   }
+}
+
+// Zero the 8 deposit cells of each particle in all 4 components (several particles may share a
+// cell: every write is the same zero).
+__global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const int32_t* __restrict__ dep,
+                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  // in cell order (the coupling pass's order) neighbouring threads zero neighbouring cells
+  const int32_t c = dep[order ? order[t] : t];
+  if (c < 0) return;
+  const uint32_t c0 = (uint32_t)c;
+  const uint32_t nodes[8] = {c0, c0 + sz, c0 + sy, c0 + sy + sz, c0 + 1, c0 + 1 + sz, c0 + 1 + sy, c0 + 1 + sy + sz};
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) pdrag[(size_t)a * n + nodes[cc]] = 0.0f;
 }
 
 __global__ void fixed_to_float_kernel(uint32_t n3, const long long* __restrict__ fix,
@@ -520,12 +539,28 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   P.drag_model = pp->drag_model;
   P.deterministic = pp->deterministic;
   P.pour = p->pour_control;
+  P.dep_cells = pp->deposit_cells;
   cudaStream_t s = (cudaStream_t)stream;
   int block = 256;
   int grid = (np + block - 1) / block;
   if (grid > 152 * 16) grid = 152 * 16;
   couple_kernel<<<grid, block, 0, s>>>(P, pos, vel, diameter, drag_old, active, np, order, u, pdrag,
                                        (unsigned long long*)pdrag_fix, u_at_particle);
+  count_launch();
+  POG_TRY_CUDA(cudaGetLastError());
+  return POG_OK;
+}
+
+int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cells, int np, const int32_t* order,
+                                float* pdrag, void* stream) {
+  int rc = pog_validate_params(p);
+  if (rc) return rc;
+  if (np < 0) return set_error(POG_E_ARG, "np=%d", np);
+  if (np == 0) return POG_OK;
+  if (!deposit_cells || !pdrag) return set_error(POG_E_ARG, "NULL pointer");
+  const uint32_t sy = (uint32_t)p->nx, sz = (uint32_t)p->nx * (uint32_t)p->ny;
+  clear_deposit_kernel<<<(np + 255) / 256, 256, 0, (cudaStream_t)stream>>>(sz * (uint32_t)p->nz, sy, sz,
+                                                                          deposit_cells, order, np, pdrag);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;

@@ -266,6 +266,7 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
          # rho/u as the last step left them (the moments the next coupling pass reads) and the
          # particle drag deposit of the last coupled step
          "rho": s._rho.cpu().numpy(), "u": s._u.cpu().numpy(), "macro_dirty": np.int8(s._macro_dirty),
+         "u_stale": np.int8(s._u_stale),
          "pdrag": s._pdrag.cpu().numpy(), "pdrag_active": np.int8(s._pdrag_active),
          "phase": s._phase.cpu().numpy(), "rho_external": np.int8(s._rho_external)}
     if s._porosity is not None:
@@ -313,6 +314,7 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     s._rho.copy_(torch.from_numpy(z["rho"]))
     s._u.copy_(torch.from_numpy(z["u"]))
     s._pdrag.copy_(torch.from_numpy(z["pdrag"]))
+    s._pdrag_owner = None
     s._pdrag_active = bool(z["pdrag_active"])
     if "phase" in z:
         s._phase.copy_(torch.from_numpy(z["phase"]))
@@ -324,6 +326,7 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     s.t = int(z["t"])
     s.step_count = int(z["step_count"])
     s._macro_dirty = bool(z["macro_dirty"])
+    s._u_stale = bool(z["u_stale"]) if "u_stale" in z else False
     if particles is not None and "p_count" in z:
         p = particles
         p.count = int(z["p_count"])

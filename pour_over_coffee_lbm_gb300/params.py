@@ -54,6 +54,7 @@ class PogParticleParams(ctypes.Structure):
         ("drag_model", ctypes.c_int32), ("deterministic", ctypes.c_int32),
         ("wall_margin", ctypes.c_float), ("wall_pullback", ctypes.c_float),
         ("wall_damping", ctypes.c_float), ("z_floor", ctypes.c_float),
+        ("deposit_cells", ctypes.c_void_p),
     ]
 
 

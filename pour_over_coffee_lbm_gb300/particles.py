@@ -82,6 +82,10 @@ class CoffeeParticleSystem:
         self._perm = torch.arange(n, dtype=torch.int32, device=dev)
         self._scratch = torch.empty(int(self.lib.pog_particles_bin_scratch_bytes(n)), dtype=torch.uint8, device=dev)
         self._fix = None
+        # base cell of each particle's last drag deposit (-1: none), for the sparse clear
+        self._dep = torch.full((n,), -1, dtype=torch.int32, device=dev)
+        self._dep_n = 0
+        self._dep_valid = False
         self.count = 0
         self._since_sort = None
         self._solver = None
@@ -105,6 +109,7 @@ class CoffeeParticleSystem:
         self._active.zero_()
         self._active[:n].copy_(torch.as_tensor(np.asarray(active, np.int32)))
         self._drag_old.zero_()
+        self._dep_valid = False
         if drag_old is not None:
             self._drag_old[:, :n].copy_(torch.as_tensor(np.asarray(drag_old, np.float32)))
         self._since_sort = None
@@ -139,6 +144,7 @@ class CoffeeParticleSystem:
         pp = pc.to_c()
         pp.dt = float(dt)
         pp.relaxation = float(relaxation_factor)
+        pp.deposit_cells = self._dep.data_ptr()
         f_out = pdrag if pdrag is not None else solver._pdrag
         fix = None
         if pc.deterministic:
@@ -159,6 +165,18 @@ class CoffeeParticleSystem:
             f_out.add_(tmp)
         self._solver = solver
         self._since_sort = (self._since_sort or 0) + 1
+        self._dep_n = n
+        self._dep_valid = True
+
+    def clear_deposit(self, solver, pdrag: Optional[torch.Tensor] = None) -> None:
+        """Zero the cells of the last couple() deposit in pdrag (default: the solver's), so a
+        deposit field that held only that deposit is all zeros again."""
+        if not self._dep_valid or self._dep_n == 0:
+            return
+        f_out = pdrag if pdrag is not None else solver._pdrag
+        _lib.check(self.lib.pog_particles_clear_deposit(solver._p, _lib.ptr(self._dep), self._dep_n,
+                                                        _lib.ptr(self._perm), _lib.ptr(f_out),
+                                                        _lib.stream_handle()))
 
     # ---- reference accessors -----------------------------------------------------------------
     @property

@@ -158,6 +158,7 @@ class GB300LBMSolver:
         # particle drag deposit (Kp, Kv_x, Kv_y, Kv_z) written by the coupling pass
         self._pdrag = torch.zeros((4,) + shape, dtype=torch.float32, device=dev)
         self._pdrag_active = False
+        self._pdrag_owner = None  # the particle system whose last deposit is all _pdrag holds
         self._phase = torch.ones(shape, dtype=torch.float32, device=dev)
         self._red = torch.zeros(RED_COUNT, dtype=torch.float64, device=dev)
         self._porosity = None
@@ -168,6 +169,7 @@ class GB300LBMSolver:
         # refresh of u then leaves it alone, as the reference's lbm.rho
         self._rho_external = False
         self._rho_scratch = None
+        self._u_stale = False  # u must be recomputed (a force input changed), rho is current
         if porosity is not None:
             self.set_porosity(porosity)
         self.t = 0
@@ -189,10 +191,13 @@ class GB300LBMSolver:
         _lib.check(self.lib.pog_build_flags(self._p, _lib.ptr(self._flags), self._s()))
 
     def _refresh_macro(self):
-        if not self._macro_dirty:
+        """Recompute the moments the next read needs: rho and u when the state changed since they
+        were taken (_macro_dirty), u alone when only a force input changed (_u_stale; rho does
+        not depend on forces), never a density a plugin wrote (_rho_external)."""
+        if not (self._macro_dirty or self._u_stale):
             return
         rho_out = self._rho
-        if self._rho_external:
+        if self._rho_external or not self._macro_dirty:
             if self._rho_scratch is None:
                 self._rho_scratch = torch.empty_like(self._rho)
             rho_out = self._rho_scratch
@@ -201,6 +206,7 @@ class GB300LBMSolver:
                                             _lib.ptr(self._pdrag) if self._pdrag_active else None,
                                             _lib.ptr(rho_out), _lib.ptr(self._u), self._s()))
         self._macro_dirty = False
+        self._u_stale = False
 
     def _current_rho(self) -> torch.Tensor:
         """The density field as the reference's lbm.rho holds it: a plugin-written density until
@@ -211,7 +217,7 @@ class GB300LBMSolver:
 
     def _force_written(self):
         self._force_active = True
-        self._macro_dirty = True
+        self._u_stale = True
 
     # ---- fields (reference attribute surface) ---------------------------------------------
     @property
@@ -263,11 +269,13 @@ class GB300LBMSolver:
         return FieldView(self._phase, on_write=self._phase_written)
 
     def _phase_written(self):
-        self._macro_dirty = True
+        self._u_stale = True
 
     @property
     def body_force(self) -> FieldView:
-        return FieldView(self._force, ncomp=3, on_write=self._force_written)
+        # any access may write the tensor in place: the field then counts as live (an inactive
+        # field is skipped by the step and by clear_body_force, which relies on it being zero)
+        return FieldView(self._force, ncomp=3, refresh=self._force_written, on_write=self._force_written)
 
     @property
     def les_mask(self) -> FieldView:
@@ -302,6 +310,8 @@ class GB300LBMSolver:
             for b in self._ul:
                 b.copy_(self._u)
         self._macro_dirty = False
+        self._u_stale = False
+        self._rho_external = False
         self._mass0 = float(self._rho[fluid].double().sum())
 
     def init_fields(self) -> None:
@@ -341,7 +351,7 @@ class GB300LBMSolver:
         if a.shape == (self.NX, self.NY, self.NZ):
             a = a.transpose(2, 1, 0)
         self._porosity = torch.as_tensor(np.ascontiguousarray(a).reshape(self.NZ, self.NY, self.NX)).to(self.device)
-        self._macro_dirty = True
+        self._u_stale = True
 
     # ---- stepping -------------------------------------------------------------------------
     def run(self, nsteps: int, reduce: bool = False, want_macro: bool = False) -> Optional[torch.Tensor]:
@@ -372,6 +382,7 @@ class GB300LBMSolver:
         # that step started from, as the reference's solver.rho/u after step()); otherwise they
         # are recomputed from the current state when read.
         self._macro_dirty = not want_macro
+        self._u_stale = False
         self._rho_external = False
         return self._red if reduce else None
 
@@ -388,6 +399,7 @@ class GB300LBMSolver:
         return None
 
     def compute_macroscopic_quantities(self) -> None:
+        self._rho_external = False
         self._macro_dirty = True
         self._refresh_macro()
 
@@ -403,9 +415,11 @@ class GB300LBMSolver:
             particle_system.update(self)
 
     def clear_body_force(self) -> None:
-        self._force.zero_()
-        self._force_active = False
-        self._macro_dirty = True
+        # an inactive force field is all zeros already (every writer marks it active)
+        if self._force_active:
+            self._force.zero_()
+            self._force_active = False
+            self._u_stale = True
 
     def add_force_term(self, force_field: Any) -> None:
         """body_force += force_field ((NX,NY,NZ,3) array/tensor or a FieldView)."""
@@ -425,8 +439,14 @@ class GB300LBMSolver:
         reduce=True returns the step's FP64 sums (mass, momentum, outflow, non-finite)."""
         self._refresh_macro()  # the coupling reads u of the current state
         self.clear_body_force()  # legacy/lbm_solver.py:1489
-        self._pdrag.zero_()
+        # the deposit field holds only this particle system's previous deposit: zero those
+        # cells instead of the whole field
+        if self._pdrag_owner is particle_system and particle_system._dep_valid:
+            particle_system.clear_deposit(self, self._pdrag)
+        else:
+            self._pdrag.zero_()
         particle_system.couple(self, dt=dt, relaxation_factor=relaxation_factor, pdrag=self._pdrag)
+        self._pdrag_owner = particle_system
         self._pdrag_active = True
         return self.run(1, want_macro=True, reduce=reduce)
 
@@ -467,7 +487,7 @@ class GB300LBMSolver:
                 raise ValueError("pour block must be a contiguous CUDA float32 tensor of 20 values")
         self._pour_ctl = block
         self._p.pour_control = None if block is None else block.data_ptr()
-        self._macro_dirty = True
+        self._u_stale = True
 
     def set_phase_field(self, phase: Optional[torch.Tensor], tau_air: Optional[float] = None) -> None:
         """Let the step read a phase indicator (CUDA float32, one value per cell, 0 air .. 1 water):
@@ -482,7 +502,7 @@ class GB300LBMSolver:
         self._phase_attached = phase
         self._p.phase = None if phase is None else phase.data_ptr()
         _lib.check(self.lib.pog_validate_params(self._p))
-        self._macro_dirty = True
+        self._u_stale = True
 
     def set_filter_blockage(self, blockage: Optional[torch.Tensor]) -> None:
         """Attach the filter-paper blockage field b (CUDA float32, one value per cell, written by
@@ -494,7 +514,7 @@ class GB300LBMSolver:
                 raise ValueError("filter blockage must be a contiguous CUDA float32 tensor of ncell values")
         self._blockage = blockage
         self._p.filter_blockage = None if blockage is None else blockage.data_ptr()
-        self._macro_dirty = True
+        self._u_stale = True
 
     def capture(self, nsteps: int, particle_system=None, dt: float = 1.0,
                 relaxation_factor: float = 0.8) -> "StepGraph":
@@ -632,6 +652,7 @@ class StepGraph:
         s.t += self.nsteps
         s.step_count += self.nsteps
         s._macro_dirty = self.ps is None
+        s._u_stale = False
         s._rho_external = False
         if self.ps is not None:
             self.ps._since_sort = self._ps_after

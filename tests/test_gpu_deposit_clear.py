@@ -1,0 +1,39 @@
+"""The sparse clear of the particle drag deposit (pog_particles_clear_deposit) leaves the deposit
+field exactly as a full-field fill does: after it the field is all zeros, and a deterministic
+coupled run that clears only the particles' cells is bit-identical to one that zeroes the whole
+field every step."""
+import pytest
+import torch
+
+from pour_over_coffee_lbm_gb300.params import LatticeConfig, ParticleConfig
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("deterministic", [False, True])
+def test_sparse_deposit_clear_is_exact(cuda, deterministic):
+    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    cfg = LatticeConfig(nx=40, ny=40, nz=48, band_thickness=3.0)
+    pc = ParticleConfig(count=3000, deterministic=deterministic)
+
+    def run(full_fill):
+        s = GB300LBMSolver(cfg)
+        ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
+        ps.seed()
+        for _ in range(12):
+            if full_fill:
+                s._pdrag_owner = None
+            s.step_with_two_way_coupling(ps)
+        torch.cuda.synchronize()
+        return s, ps
+
+    a, pa = run(False)
+    if deterministic:  # float atomics make the other mode differ run to run anyway
+        b, pb = run(True)
+        assert torch.equal(a._f, b._f) and torch.equal(pa._pos, pb._pos)
+    # after the last step's clear the field holds the last deposit only
+    dep = a._pdrag.clone()
+    pa.clear_deposit(a)
+    torch.cuda.synchronize()
+    assert dep.abs().sum() > 0 and a._pdrag.abs().sum().item() == 0.0
