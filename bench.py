@@ -148,32 +148,40 @@ def time_graph(graph, replays):
     return start.elapsed_time(end) / 1e3
 
 
-def kernel_roofline(cfg, steps, peak):
-    """Average duration of the fused LBM step kernel alone (same arguments as inside the coupled
-    step: particle drag deposit read, rho/u write), over `steps` graph-replayed launches."""
+def kernel_roofline(cfg, pc, steps, peak):
+    """Average duration of the fused LBM step kernel alone with the arguments it has inside the
+    coupled step (the particle drag deposit and its cell mask of a real coupling pass, rho/u
+    written), over `steps` graph-replayed launches."""
     import torch
+    from pour_over_coffee_lbm_gb300.params import CELL_SOLID
+    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     s = GB300LBMSolver(cfg)
-    s._pdrag.uniform_(0.0, 1e-3)
-    s._pdrag_active = True
-    for _ in range(4):
-        s.run(1, want_macro=True)
+    ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
+    ps.seed()
+    for _ in range(6):
+        s.step_with_two_way_coupling(ps)
     torch.cuda.synchronize()
     g = GraphOfSteps(s, GRAPH_STEPS)
     time_graph(g, 2)
     reps = max(1, steps // GRAPH_STEPS)
     dt = time_graph(g, reps)
     per_launch = dt / (reps * GRAPH_STEPS)
-    nf = fluid_cells(s.flags)
+    fluid = (s._flags.reshape(-1) & CELL_SOLID) == 0
+    nf = int(fluid.sum().item())
+    bits = ((s._dmask.view(-1, 1) >> torch.arange(32, device=s._dmask.device, dtype=torch.int32)) & 1).reshape(-1)
+    nd = int((bits[:s.n].bool() & fluid).sum().item())
     esize = s._f.element_size()
-    bytes_per_launch = nf * (2 * 19 * esize + 16 + 4 + 12) + s.n * 4
+    # per fluid cell: 19 populations read + written, rho/u written; per deposit cell: the 16 B
+    # deposit read; per cell: the 4 B flag word and one bit of the deposit mask
+    bytes_per_launch = nf * (2 * 19 * esize + 4 + 12) + nd * 16 + s.n * 4 + s.n // 8
     achieved = bytes_per_launch / per_launch / 1e9
     out = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0], "unit": "GB/s",
            "frac": round(achieved / peak[0], 4), "peak_source": peak[1],
-           "kernel": "aa_step_kernel (fused collide-stream, particle drag read, rho/u write)",
+           "kernel": "aa_step_kernel (fused collide-stream, particle drag read at deposit cells, rho/u write)",
            "kernel_us": round(per_launch * 1e6, 2), "algorithmic_bytes_per_launch": bytes_per_launch,
-           "fluid_cells": nf, "cells": s.n}
-    del s, g
+           "fluid_cells": nf, "deposit_cells": nd, "cells": s.n}
+    del s, g, ps
     return out
 
 
@@ -636,7 +644,7 @@ def run_ours(args):
     e2e_ok = bool(torch.isfinite(red_h[:, :5]).all()) and float(red_h[:, 5].sum()) == 0.0
     solver.set_inlet_control(None)
 
-    roof = kernel_roofline(cfg, max(200, K), peak)
+    roof = kernel_roofline(cfg, pc, max(200, K), peak)
     traffic_path = os.path.join(ROOT, "profiles", "aa_step_traffic.json")
     roof["traffic"] = None
     if os.path.exists(traffic_path):

@@ -133,6 +133,11 @@ typedef struct pog_params {
    * else tau_air; nu_sgs = 0 where |phase| < 0.9. */
   const float* phase;
   float tau_air;            /* molecular relaxation time of the air phase (TAU_AIR)           */
+  /* Optional DEVICE bit mask [ceil(ncell/32)] or NULL: bit c set where the particle drag deposit
+   * pdrag may be nonzero (pog_particles_couple sets the bits of the cells it deposits into,
+   * pog_particles_clear_deposit clears them).  With a mask the step reads pdrag only at set bits
+   * and takes zero elsewhere; the caller keeps pdrag zero wherever the bit is clear. */
+  const uint32_t* deposit_mask;
 } pog_params;
 
 /* Pour-nozzle block, floats (PrecisePouringSystem, src/physics/precise_pouring.py:12-193):
@@ -194,6 +199,9 @@ typedef struct pog_particle_params {
    * corner) of each particle's 8-cell drag deposit, -1 for a particle that deposited nothing, so
    * that pog_particles_clear_deposit can zero exactly those cells after the lattice step. */
   int32_t* deposit_cells;
+  /* Optional DEVICE bit mask [ceil(ncell/32)] or NULL: the coupling pass sets bit c for every
+   * cell it deposits into (see pog_params.deposit_mask). */
+  uint32_t* deposit_mask;
 } pog_particle_params;
 
 /* ---- library ------------------------------------------------------------------------------- */
@@ -406,9 +414,10 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
  * particle whose deposit_cells entry (from pog_particles_couple) is >= 0: after the lattice step
  * has read the deposit, this returns pdrag to all zeros at the cost of the particles' cells
  * instead of a full-field fill.  order (nullable): the coupling pass's particle order, so that
- * neighbouring threads write neighbouring cells. */
+ * neighbouring threads write neighbouring cells.  deposit_mask (nullable): the cells' bits are
+ * cleared too. */
 int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cells, int np,
-                                const int32_t* order, float* pdrag, void* stream);
+                                const int32_t* order, float* pdrag, uint32_t* deposit_mask, void* stream);
 /* pdrag[a][c] = pdrag_fix[a][c] * 2^-32, a = 0..3 (deterministic-mode conversion). */
 int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* pdrag,
                         void* stream);

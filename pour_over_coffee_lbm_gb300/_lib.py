@@ -50,7 +50,7 @@ SIGNATURES = [
     ("pog_particles_bin_scratch_bytes", ctypes.c_size_t, [_i]),
     ("pog_particles_bin", _i, [_P, _v, _v, _i, _v, _v, _v, _v]),
     ("pog_particles_couple", _i, [_P, _PP, _v, _v, _v, _v, _v, _i, _v, _v, _v, _v, _v, _v]),
-    ("pog_particles_clear_deposit", _i, [_P, _v, _i, _v, _v, _v]),
+    ("pog_particles_clear_deposit", _i, [_P, _v, _i, _v, _v, _v, _v]),
     ("pog_drag_from_fixed", _i, [_P, _v, _v, _v]),
     ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_device_status", _i, [_i]),

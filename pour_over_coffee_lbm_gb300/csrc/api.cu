@@ -84,6 +84,7 @@ KParams make_kparams(const pog_params* p) {
   k.blockage = p->filter_blockage;
   k.phase = p->phase;
   k.tau_air = p->tau_air;
+  k.dmask = p->deposit_mask;
   return k;
 }
 

@@ -225,6 +225,8 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   // Particle drag deposit: F_p = Kv - Kp u with u implicit.  v is the velocity with every
   // explicit force, A the implicit factor (1 without particles).
   C Kp = (C)0, Kvx = (C)0, Kvy = (C)0, Kvz = (C)0;
+  // with a deposit mask only the cells the particles deposited into are read (zero elsewhere)
+  if (pdrag && kp.dmask && !((kp.dmask[c >> 5] >> (c & 31u)) & 1u)) pdrag = nullptr;
   if (pdrag) {
     Kp = (C)pdrag[c];
     Kvx = (C)pdrag[kp.n + c];

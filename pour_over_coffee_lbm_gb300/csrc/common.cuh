@@ -65,6 +65,7 @@ struct KParams {
   const float* blockage;   // device filter-paper blockage b [n] or null
   const float* phase;      // device phase indicator [n] (0 air, 1 water) or null
   float tau_air;
+  const uint32_t* dmask;   // device bit mask of the cells with a particle deposit, or null
 };
 
 KParams make_kparams(const pog_params* p);

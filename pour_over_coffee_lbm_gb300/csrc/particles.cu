@@ -188,6 +188,7 @@ struct PKParams {
   int drag_model, deterministic;
   const float* pour;  // device pour-nozzle block or null
   int32_t* dep_cells;  // device [np]: base cell of each particle's deposit (-1: none) or null
+  uint32_t* dmask;     // device bit mask of the deposited cells or null
 };
 
 // Impact force of the pour stream on a particle at (x, y, z) (create_water_impact_force,
@@ -386,6 +387,7 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
     // with the gather weights at the pre-update position; the lattice step applies the
     // particle force on the fluid, Kv - Kp u, implicitly in u.
     dep_ok = __shfl_sync(0xffffffffu, dep_ok, lead);
+    if (dep_ok && P.dmask) atomicOr(P.dmask + (node >> 5), 1u << (node & 31u));
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       const float contrib = wr * __shfl_sync(0xffffffffu, dep[a], lead);
@@ -404,7 +406,8 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
 // Zero the 8 deposit cells of each particle in all 4 components (several particles may share a
 // cell: every write is the same zero).
 __global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const int32_t* __restrict__ dep,
-                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag) {
+                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag,
+                                     uint32_t* __restrict__ dmask) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= np) return;
   // in cell order (the coupling pass's order) neighbouring threads zero neighbouring cells
@@ -416,6 +419,10 @@ __global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int cc = 0; cc < 8; ++cc) pdrag[(size_t)a * n + nodes[cc]] = 0.0f;
+  if (dmask) {
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) atomicAnd(dmask + (nodes[cc] >> 5), ~(1u << (nodes[cc] & 31u)));
+  }
 }
 
 __global__ void fixed_to_float_kernel(uint32_t n3, const long long* __restrict__ fix,
@@ -546,6 +553,7 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   P.deterministic = pp->deterministic;
   P.pour = p->pour_control;
   P.dep_cells = pp->deposit_cells;
+  P.dmask = pp->deposit_mask;
   cudaStream_t s = (cudaStream_t)stream;
   int block = 256;
   long long want = ((long long)np * CPL_LANES + block - 1) / block;
@@ -558,7 +566,7 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
 }
 
 int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cells, int np, const int32_t* order,
-                                float* pdrag, void* stream) {
+                                float* pdrag, uint32_t* deposit_mask, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
   if (np < 0) return set_error(POG_E_ARG, "np=%d", np);
@@ -566,7 +574,8 @@ int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cell
   if (!deposit_cells || !pdrag) return set_error(POG_E_ARG, "NULL pointer");
   const uint32_t sy = (uint32_t)p->nx, sz = (uint32_t)p->nx * (uint32_t)p->ny;
   clear_deposit_kernel<<<(np + 255) / 256, 256, 0, (cudaStream_t)stream>>>(sz * (uint32_t)p->nz, sy, sz,
-                                                                          deposit_cells, order, np, pdrag);
+                                                                          deposit_cells, order, np, pdrag,
+                                                                          deposit_mask);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;

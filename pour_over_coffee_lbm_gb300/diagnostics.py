@@ -268,7 +268,8 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
          "rho": s._rho.cpu().numpy(), "u": s._u.cpu().numpy(), "macro_dirty": np.int8(s._macro_dirty),
          "u_stale": np.int8(s._u_stale),
          "pdrag": s._pdrag.cpu().numpy(), "pdrag_active": np.int8(s._pdrag_active),
-         "phase": s._phase.cpu().numpy(), "rho_external": np.int8(s._rho_external)}
+         "phase": s._phase.cpu().numpy(), "rho_external": np.int8(s._rho_external),
+         "deposit_mask": s._dmask.cpu().numpy()}
     if s._porosity is not None:
         d["porosity"] = s._porosity.cpu().numpy()
     if s._ul is not None:
@@ -315,6 +316,10 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     s._u.copy_(torch.from_numpy(z["u"]))
     s._pdrag.copy_(torch.from_numpy(z["pdrag"]))
     s._pdrag_owner = None
+    if "deposit_mask" in z:
+        s._dmask.copy_(torch.from_numpy(z["deposit_mask"]))
+    else:  # every cell may hold a deposit
+        s._dmask.fill_(-1)
     s._pdrag_active = bool(z["pdrag_active"])
     if "phase" in z:
         s._phase.copy_(torch.from_numpy(z["phase"]))

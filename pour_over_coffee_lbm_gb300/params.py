@@ -45,6 +45,7 @@ class PogParams(ctypes.Structure):
         ("pour_control", ctypes.c_void_p),
         ("filter_blockage", ctypes.c_void_p),
         ("phase", ctypes.c_void_p), ("tau_air", ctypes.c_float),
+        ("deposit_mask", ctypes.c_void_p),
     ]
 
 
@@ -54,7 +55,7 @@ class PogParticleParams(ctypes.Structure):
         ("drag_model", ctypes.c_int32), ("deterministic", ctypes.c_int32),
         ("wall_margin", ctypes.c_float), ("wall_pullback", ctypes.c_float),
         ("wall_damping", ctypes.c_float), ("z_floor", ctypes.c_float),
-        ("deposit_cells", ctypes.c_void_p),
+        ("deposit_cells", ctypes.c_void_p), ("deposit_mask", ctypes.c_void_p),
     ]
 
 

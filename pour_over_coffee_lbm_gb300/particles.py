@@ -131,10 +131,11 @@ class CoffeeParticleSystem:
         return self._keys[:n], (self._perm[:n] if sort else None)
 
     def couple(self, solver, dt: float = 1.0, relaxation_factor: float = 0.8,
-               pdrag: Optional[torch.Tensor] = None):
+               pdrag: Optional[torch.Tensor] = None, deposit_mask: Optional[torch.Tensor] = None):
         """One coupling pass against solver's current velocity field: drag, under-relaxation,
         integration, and the drag deposit (Kp, Kv) added into `pdrag` ([4, NZ, NY, NX], not
-        cleared here) for the implicit fluid-side force of the next lattice step."""
+        cleared here) for the implicit fluid-side force of the next lattice step.  deposit_mask
+        (int32 [ceil(ncell/32)]): the bits of the deposited cells are set."""
         n = self.count
         if n == 0:
             return
@@ -145,6 +146,7 @@ class CoffeeParticleSystem:
         pp.dt = float(dt)
         pp.relaxation = float(relaxation_factor)
         pp.deposit_cells = self._dep.data_ptr()
+        pp.deposit_mask = None if deposit_mask is None else deposit_mask.data_ptr()
         f_out = pdrag if pdrag is not None else solver._pdrag
         fix = None
         if pc.deterministic:
@@ -168,14 +170,17 @@ class CoffeeParticleSystem:
         self._dep_n = n
         self._dep_valid = True
 
-    def clear_deposit(self, solver, pdrag: Optional[torch.Tensor] = None) -> None:
-        """Zero the cells of the last couple() deposit in pdrag (default: the solver's), so a
-        deposit field that held only that deposit is all zeros again."""
+    def clear_deposit(self, solver, pdrag: Optional[torch.Tensor] = None,
+                      deposit_mask: Optional[torch.Tensor] = None) -> None:
+        """Zero the cells of the last couple() deposit in pdrag (default: the solver's) and clear
+        their bits in deposit_mask (default: the solver's), so a deposit field that held only
+        that deposit is all zeros again."""
         if not self._dep_valid or self._dep_n == 0:
             return
         f_out = pdrag if pdrag is not None else solver._pdrag
+        mask = deposit_mask if deposit_mask is not None else getattr(solver, "_dmask", None)
         _lib.check(self.lib.pog_particles_clear_deposit(solver._p, _lib.ptr(self._dep), self._dep_n,
-                                                        _lib.ptr(self._perm), _lib.ptr(f_out),
+                                                        _lib.ptr(self._perm), _lib.ptr(f_out), _lib.ptr(mask),
                                                         _lib.stream_handle()))
 
     # ---- reference accessors -----------------------------------------------------------------

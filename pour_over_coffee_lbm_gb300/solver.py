@@ -159,6 +159,9 @@ class GB300LBMSolver:
         self._pdrag = torch.zeros((4,) + shape, dtype=torch.float32, device=dev)
         self._pdrag_active = False
         self._pdrag_owner = None  # the particle system whose last deposit is all _pdrag holds
+        # one bit per cell: set where _pdrag may be nonzero (the step reads the deposit there only)
+        self._dmask = torch.zeros((self.n + 31) // 32, dtype=torch.int32, device=dev)
+        self._p.deposit_mask = self._dmask.data_ptr()
         self._phase = torch.ones(shape, dtype=torch.float32, device=dev)
         self._red = torch.zeros(RED_COUNT, dtype=torch.float64, device=dev)
         self._porosity = None
@@ -442,10 +445,12 @@ class GB300LBMSolver:
         # the deposit field holds only this particle system's previous deposit: zero those
         # cells instead of the whole field
         if self._pdrag_owner is particle_system and particle_system._dep_valid:
-            particle_system.clear_deposit(self, self._pdrag)
+            particle_system.clear_deposit(self, self._pdrag, self._dmask)
         else:
             self._pdrag.zero_()
-        particle_system.couple(self, dt=dt, relaxation_factor=relaxation_factor, pdrag=self._pdrag)
+            self._dmask.zero_()
+        particle_system.couple(self, dt=dt, relaxation_factor=relaxation_factor, pdrag=self._pdrag,
+                               deposit_mask=self._dmask)
         self._pdrag_owner = particle_system
         self._pdrag_active = True
         return self.run(1, want_macro=True, reduce=reduce)

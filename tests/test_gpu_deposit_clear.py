@@ -37,3 +37,4 @@ def test_sparse_deposit_clear_is_exact(cuda, deterministic):
     pa.clear_deposit(a)
     torch.cuda.synchronize()
     assert dep.abs().sum() > 0 and a._pdrag.abs().sum().item() == 0.0
+    assert int((a._dmask != 0).sum().item()) == 0
