@@ -406,8 +406,7 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
 // Zero the 8 deposit cells of each particle in all 4 components (several particles may share a
 // cell: every write is the same zero).
 __global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const int32_t* __restrict__ dep,
-                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag,
-                                     uint32_t* __restrict__ dmask) {
+                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= np) return;
   // in cell order (the coupling pass's order) neighbouring threads zero neighbouring cells
@@ -419,10 +418,6 @@ __global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int cc = 0; cc < 8; ++cc) pdrag[(size_t)a * n + nodes[cc]] = 0.0f;
-  if (dmask) {
-#pragma unroll
-    for (int cc = 0; cc < 8; ++cc) atomicAnd(dmask + (nodes[cc] >> 5), ~(1u << (nodes[cc] & 31u)));
-  }
 }
 
 __global__ void fixed_to_float_kernel(uint32_t n3, const long long* __restrict__ fix,
@@ -574,10 +569,14 @@ int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cell
   if (!deposit_cells || !pdrag) return set_error(POG_E_ARG, "NULL pointer");
   const uint32_t sy = (uint32_t)p->nx, sz = (uint32_t)p->nx * (uint32_t)p->ny;
   clear_deposit_kernel<<<(np + 255) / 256, 256, 0, (cudaStream_t)stream>>>(sz * (uint32_t)p->nz, sy, sz,
-                                                                          deposit_cells, order, np, pdrag,
-                                                                          deposit_mask);
+                                                                          deposit_cells, order, np, pdrag);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
+  // once the deposit is gone no cell holds one: clearing the whole mask (ncell / 8 bytes) is
+  // cheaper than clearing its bits one atomic at a time
+  if (deposit_mask)
+    POG_TRY_CUDA(cudaMemsetAsync(deposit_mask, 0, (((size_t)sz * (uint32_t)p->nz + 31) / 32) * sizeof(uint32_t),
+                                 (cudaStream_t)stream));
   return POG_OK;
 }
 
