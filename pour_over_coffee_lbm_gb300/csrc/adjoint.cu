@@ -51,6 +51,28 @@ __device__ __forceinline__ void eq_vjp(const C lam[19], C rho, C ux, C uy, C uz,
   buz = bz;
 }
 
+// eq_vjp for lam_q = a_q - b_q (not stored)
+template <typename C>
+__device__ __forceinline__ void eq_vjp_diff(const C a[19], const C b[19], C rho, C ux, C uy, C uz, C& brho,
+                                            C& bux, C& buy, C& buz) {
+  C br = 0, bx = 0, by = 0, bz = 0;
+  const C usq = ux * ux + uy * uy + uz * uz;
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    const C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
+    const C wl = (C)wd(q) * (a[q] - b[q]);
+    br += wl * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - (C)1.5 * usq);
+    const C g = wl * rho * ((C)3 + (C)9 * eu);
+    bx += g * (C)cx(q) - wl * rho * (C)3 * ux;
+    by += g * (C)cy(q) - wl * rho * (C)3 * uy;
+    bz += g * (C)cz(q) - wl * rho * (C)3 * uz;
+  }
+  brho = br;
+  bux = bx;
+  buy = by;
+  buz = bz;
+}
+
 template <typename C>
 __device__ __forceinline__ C chebyshev_T(int k, C s) {
   C t0 = (C)1, t1 = s;
@@ -63,19 +85,105 @@ __device__ __forceinline__ C chebyshev_T(int k, C s) {
   return t1;
 }
 
+// Inlet cell c (f* = feq(rho, (0, 0, u_z(a)))): bar f (all directions equal) from the pulled
+// lam*, and the cell's contributions to dJ/da_k added into g[16].
+template <typename C>
+__device__ __forceinline__ C adj_inlet_cell(const KParams& kp, uint32_t c, const C ls[19], C rho, double g[16]) {
+  const C uz = inlet_uz<C>(kp, c);
+  C brho, bux, buy, buz;
+  eq_vjp<C>(ls, rho, (C)0, (C)0, uz, brho, bux, buy, buz);
+  // uz = u_inlet (1 + sum a_k T_k(s)), s = 2 r / R - 1
+  const uint32_t i = c % kp.nx, j = (c / kp.nx) % kp.ny;
+  const C dx = (C)i - (C)kp.cxf, dy = (C)j - (C)kp.cyf;
+  const C r = sqrt(dx * dx + dy * dy);
+  const C R = (C)kp.inlet_R;
+  const C s = R > (C)0 ? (C)2 * r / R - (C)1 : (C)0;
+  C t0 = (C)1, t1 = s;
+  const C ub = (C)(kp.inlet_ctl ? kp.inlet_ctl[0] : kp.u_inlet);
+  g[0] += (double)(buz * ub);
+  g[1] += (double)(buz * ub * t1);
+#pragma unroll
+  for (int k = 2; k < POG_INLET_NCOEF; ++k) {
+    const C t2 = (C)2 * s * t1 - t0;
+    g[k] += (double)(buz * ub * t2);
+    t0 = t1;
+    t1 = t2;
+  }
+  return brho;
+}
+
+// The pull of the transposed streaming and the density of cell c (shared by both kernels).
 template <int S>
-__global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
+__device__ __forceinline__ void adj_pull(const KParams& kp, const typename Store<S>::E* __restrict__ lam_next,
+                                         uint32_t c, uint32_t fl, typename Store<S>::C ls[19]) {
+  using C = typename Store<S>::C;
+  const uint32_t n = kp.n;
+#pragma unroll
+  for (int q = 0; q < 19; ++q) {
+    const uint32_t dst = c + (uint32_t)kp.off[q];
+    const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
+    ls[q] = wall ? (C)lam_next[(uint32_t)opp(q) * n + c] : (C)lam_next[(uint32_t)q * n + dst];
+  }
+}
+
+// The inlet disk's plane (k = nz - 2, where pog_build_flags puts the inlet): one block, so the
+// dJ/da_k sums have a fixed order and repeat bit for bit.
+template <int S>
+__global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
-    const uint32_t* __restrict__ flags, const float* __restrict__ eps,
-    double* __restrict__ grad_eps, double* __restrict__ grad_inlet) {
+    const uint32_t* __restrict__ flags, uint32_t lo, uint32_t hi, double* __restrict__ grad_inlet) {
   using St = Store<S>;
   using C = typename St::C;
   using E = typename St::E;
   const uint32_t n = kp.n;
-  double ginl[POG_INLET_NCOEF];
+  double g[POG_INLET_NCOEF];
 #pragma unroll
-  for (int k = 0; k < POG_INLET_NCOEF; ++k) ginl[k] = 0.0;
+  for (int k = 0; k < POG_INLET_NCOEF; ++k) g[k] = 0.0;
+  for (uint32_t c = lo + threadIdx.x; c < hi; c += ADJ_BLOCK) {
+    const uint32_t fl = flags[c];
+    if (!(fl & POG_CELL_INLET) || (fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
+    C ls[19];
+    adj_pull<S>(kp, lam_next, c, fl, ls);
+    C rho = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) rho += St::ld(ft, (uint32_t)q * n + c, q, (C)kp.rho0);
+    const C brho = adj_inlet_cell<C>(kp, c, ls, rho, g);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)brho;
+  }
+  if (!grad_inlet) return;
+  __shared__ double sm[POG_INLET_NCOEF][ADJ_BLOCK / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < POG_INLET_NCOEF; ++k) {
+    double x = g[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < POG_INLET_NCOEF) {
+    double x = 0.0;
+    for (int w = 0; w < ADJ_BLOCK / 32; ++w) x += sm[threadIdx.x][w];
+    grad_inlet[threadIdx.x] += x;
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint_kernel(
+    const KParams kp, const typename Store<S>::E* __restrict__ ft,
+    const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
+    const uint32_t* __restrict__ flags, const float* __restrict__ eps,
+    double* __restrict__ grad_eps, double* __restrict__ grad_inlet, uint32_t inlet_lo, uint32_t inlet_hi) {
+  using St = Store<S>;
+  using C = typename St::C;
+  using E = typename St::E;
+  const uint32_t n = kp.n;
+  // inlet cells off the inlet plane (custom flags only): shared FP64 accumulators
+  __shared__ double ginl[POG_INLET_NCOEF];
+  if (threadIdx.x < POG_INLET_NCOEF) ginl[threadIdx.x] = 0.0;
+  __syncthreads();
   for (uint32_t c = blockIdx.x * ADJ_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_BLOCK) {
     const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
@@ -83,14 +191,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
       for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)0;
       continue;
     }
+    // the inlet plane's inlet cells are done by adjoint_inlet_kernel
+    if ((fl & POG_CELL_INLET) && c >= inlet_lo && c < inlet_hi) continue;
     // 1. transpose of push streaming
     C ls[19];
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-      const uint32_t dst = c + (uint32_t)kp.off[q];
-      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
-      ls[q] = wall ? (C)lam_next[(uint32_t)opp(q) * n + c] : (C)lam_next[(uint32_t)q * n + dst];
-    }
+    adj_pull<S>(kp, lam_next, c, fl, ls);
     C f[19];
     const C rs = (C)kp.rho0;
 #pragma unroll
@@ -106,27 +211,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
     C brho = 0, bmx = 0, bmy = 0, bmz = 0;
     C bf[19];
     if (fl & POG_CELL_INLET) {
-      // f* = feq(rho, (0,0,uz(a)))
-      const C uz = inlet_uz<C>(kp, c);
-      C bux, buy, buz;
-      eq_vjp<C>(ls, rho, (C)0, (C)0, uz, brho, bux, buy, buz);
-      // uz = u_inlet (1 + sum a_k T_k(s))
-      uint32_t i = c % kp.nx, j = (c / kp.nx) % kp.ny;
-      C dx = (C)i - (C)kp.cxf, dy = (C)j - (C)kp.cyf;
-      C r = sqrt(dx * dx + dy * dy);
-      C R = (C)kp.inlet_R;
-      C s = R > (C)0 ? (C)2 * r / R - (C)1 : (C)0;
-      C t0 = (C)1, t1 = s;
-      const C ub = (C)(kp.inlet_ctl ? kp.inlet_ctl[0] : kp.u_inlet);
-      ginl[0] += (double)(buz * ub);
-      ginl[1] += (double)(buz * ub * t1);
+      double g[POG_INLET_NCOEF];
 #pragma unroll
-      for (int k = 2; k < POG_INLET_NCOEF; ++k) {
-        C t2 = (C)2 * s * t1 - t0;
-        ginl[k] += (double)(buz * ub * t2);
-        t0 = t1;
-        t1 = t2;
-      }
+      for (int k = 0; k < POG_INLET_NCOEF; ++k) g[k] = 0.0;
+      brho = adj_inlet_cell<C>(kp, c, ls, rho, g);
+#pragma unroll
+      for (int k = 0; k < POG_INLET_NCOEF; ++k) atomicAdd(&ginl[k], g[k]);
 #pragma unroll
       for (int q = 0; q < 19; ++q) bf[q] = brho;
     } else if (fl & POG_CELL_OUTLET) {
@@ -176,10 +266,13 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
         Fy = Gy - coef * uy;
         Fz = Gz - coef * uz;
       }
-      C feq[19], neq[19];
-      eq_all<C>(rho, ux, uy, uz, feq);
+      // f becomes f - f_eq in place (f itself is not needed again)
+      C* const neq = f;
+      {
+        const C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
 #pragma unroll
-      for (int q = 0; q < 19; ++q) neq[q] = f[q] - feq[q];
+        for (int q = 0; q < 19; ++q) neq[q] = f[q] - feq_q<C>(q, rho, ux, uy, uz, usq15);
+      }
       const C tau0 = (C)kp.tau;
       C tau = tau0;
       bool les_live = false;
@@ -216,13 +309,13 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
       const C A = (C)1 - (C)0.5 * omega;
       const C uF = ux * Fx + uy * Fy + uz * Fz;
       // ---- reverse ----
-      C bneq[19], bfeq[19];
+      // bar f_eq = lam* - bar neq is formed where it is used (eq_vjp_diff)
+      C* const bneq = bf;
       C bomega = 0, bA = 0;
       C bux = 0, buy = 0, buz = 0, bFx = 0, bFy = 0, bFz = 0;
 #pragma unroll
       for (int q = 0; q < 19; ++q) {
         const C lq = ls[q];
-        bfeq[q] = lq;
         bneq[q] = ((C)1 - omega) * lq;
         bomega -= lq * neq[q];
         const C ex = (C)cx(q), ey = (C)cy(q), ez = (C)cz(q);
@@ -256,16 +349,10 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
           bneq[q] += (C)(cx(q) * cx(q)) * bPxx + (C)(cy(q) * cy(q)) * bPyy + (C)(cz(q) * cz(q)) * bPzz +
                      (C)(cx(q) * cy(q)) * bPxy + (C)(cx(q) * cz(q)) * bPxz + (C)(cy(q) * cz(q)) * bPyz;
       }
-      // neq = f - feq
-#pragma unroll
-      for (int q = 0; q < 19; ++q) {
-        bf[q] = bneq[q];
-        bfeq[q] -= bneq[q];
-      }
-      // feq(rho, u)
+      // neq = f - feq: bar f = bar neq (already in bf), bar feq = lam* - bar neq
       {
         C br, bx, by, bz;
-        eq_vjp<C>(bfeq, rho, ux, uy, uz, br, bx, by, bz);
+        eq_vjp_diff<C>(ls, bneq, rho, ux, uy, uz, br, bx, by, bz);
         brho += br;
         bux += bx;
         buy += by;
@@ -335,22 +422,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_kernel(
     for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)bf[q];
   }
   if (grad_inlet) {
-    // block reduction of the 16 inlet-profile gradients (few cells contribute)
-    __shared__ double sm[POG_INLET_NCOEF][ADJ_BLOCK / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < POG_INLET_NCOEF; ++k) {
-      double x = ginl[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) sm[k][warp] = x;
-    }
     __syncthreads();
-    if (threadIdx.x < POG_INLET_NCOEF) {
-      double x = 0.0;
-      for (int w = 0; w < ADJ_BLOCK / 32; ++w) x += sm[threadIdx.x][w];
-      if (x != 0.0) atomicAdd(grad_inlet + threadIdx.x, x);
-    }
+    if (threadIdx.x < POG_INLET_NCOEF && ginl[threadIdx.x] != 0.0)
+      atomicAdd(grad_inlet + threadIdx.x, ginl[threadIdx.x]);
   }
 }
 
@@ -364,7 +438,11 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
   int want = (int)((kp.n + ADJ_BLOCK - 1) / ADJ_BLOCK);
   int g = want < grid ? want : grid;
   using E = typename Store<S>::E;
-  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, ge, gi);
+  const uint32_t lo = (kp.nz - 2u) * kp.nxny, hi = lo + kp.nxny;  // the inlet plane
+  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, ge, gi, lo, hi);
+  count_launch();
+  POG_TRY_CUDA(cudaGetLastError());
+  adjoint_inlet_kernel<S><<<1, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi, gi);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;

@@ -9,7 +9,7 @@ namespace pog {
 constexpr int PUSH_BLOCK = 256;
 
 template <int S, bool REDUCE>
-__global__ void __launch_bounds__(PUSH_BLOCK) push_step_kernel(
+__global__ void __launch_bounds__(PUSH_BLOCK, S == POG_STORE_F64 ? 1 : 4) push_step_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ fin,
     typename Store<S>::E* __restrict__ fout, const uint32_t* __restrict__ flags,
     const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
