@@ -210,6 +210,10 @@ const char* pog_last_error(void);
 /* Number of kernel launches this thread issued through the library since the last reset. */
 long long pog_launch_count(int reset);
 
+/* Zero `bytes` bytes of device memory at p, asynchronously on `stream` (the FP64 reduction block
+ * before a reducing step, without a framework's fill kernel). */
+int pog_zero(void* p, size_t bytes, void* stream);
+
 /* Check a parameter block (sizes, enum values, ranges).  Host only. */
 int pog_validate_params(const pog_params* p);
 

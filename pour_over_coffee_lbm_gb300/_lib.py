@@ -51,6 +51,7 @@ SIGNATURES = [
     ("pog_particles_bin", _i, [_P, _v, _v, _i, _v, _v, _v, _v]),
     ("pog_particles_couple", _i, [_P, _PP, _v, _v, _v, _v, _v, _i, _v, _v, _v, _v, _v, _v]),
     ("pog_particles_clear_deposit", _i, [_P, _v, _i, _v, _v, _v, _v]),
+    ("pog_zero", _i, [_v, ctypes.c_size_t, _v]),
     ("pog_drag_from_fixed", _i, [_P, _v, _v, _v]),
     ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_device_status", _i, [_i]),
@@ -95,13 +96,14 @@ def check(code: int):
 
 
 def ptr(t):
-    """Device pointer of a tensor (or None -> NULL)."""
+    """Device pointer of a tensor as an int (ctypes passes it as void*), or None -> NULL."""
     if t is None:
         return None
-    return ctypes.c_void_p(t.data_ptr())
+    return t.data_ptr()
 
 
 def stream_handle(stream=None):
+    """The CUDA stream handle (int) of `stream`, default torch's current stream."""
     import torch
     s = stream if stream is not None else torch.cuda.current_stream()
-    return ctypes.c_void_p(s.cuda_stream)
+    return s.cuda_stream

@@ -98,6 +98,12 @@ int pog_version(void) { return POG_VERSION; }
 
 const char* pog_last_error(void) { return g_err; }
 
+int pog_zero(void* p, size_t bytes, void* stream) {
+  if (!p && bytes) return set_error(POG_E_ARG, "NULL pointer");
+  if (bytes) POG_TRY_CUDA(cudaMemsetAsync(p, 0, bytes, (cudaStream_t)stream));
+  return POG_OK;
+}
+
 long long pog_launch_count(int reset) {
   long long v = g_launches;
   if (reset) g_launches = 0;

@@ -86,6 +86,8 @@ class CoffeeParticleSystem:
         self._dep = torch.full((n,), -1, dtype=torch.int32, device=dev)
         self._dep_n = 0
         self._dep_valid = False
+        self._pp = None
+        self._pp_key = None
         self.count = 0
         self._since_sort = None
         self._solver = None
@@ -142,11 +144,18 @@ class CoffeeParticleSystem:
         pc = self.pcfg
         if self._since_sort is None or (pc.sort_interval > 0 and self._since_sort >= pc.sort_interval):
             self.bin(solver, sort=True)
-        pp = pc.to_c()
-        pp.dt = float(dt)
-        pp.relaxation = float(relaxation_factor)
-        pp.deposit_cells = self._dep.data_ptr()
-        pp.deposit_mask = None if deposit_mask is None else deposit_mask.data_ptr()
+        # the parameter block is rebuilt only when one of its inputs changes
+        mptr = None if deposit_mask is None else deposit_mask.data_ptr()
+        key = (pc.density_ratio, pc.drag_model, pc.deterministic, pc.wall_margin, pc.wall_pullback,
+               pc.wall_damping, pc.z_floor, dt, relaxation_factor, mptr)
+        if self._pp_key != key:
+            pp = pc.to_c()
+            pp.dt = float(dt)
+            pp.relaxation = float(relaxation_factor)
+            pp.deposit_cells = self._dep.data_ptr()
+            pp.deposit_mask = mptr
+            self._pp, self._pp_key = pp, key
+        pp = self._pp
         f_out = pdrag if pdrag is not None else solver._pdrag
         fix = None
         if pc.deterministic:

@@ -363,9 +363,10 @@ class GB300LBMSolver:
         if nsteps <= 0:
             return None
         red = None
+        st = self._s()
         if reduce:
-            self._red.zero_()
-            red = _lib.ptr(self._red)
+            red = self._red.data_ptr()
+            _lib.check(self.lib.pog_zero(red, self._red.numel() * 8, st))
         stencil = self.cfg.les_mode == LES_STENCIL
         up = _lib.ptr(self._ul[0]) if stencil else None
         un = _lib.ptr(self._ul[1]) if stencil else None
@@ -376,7 +377,7 @@ class GB300LBMSolver:
             _lib.ptr(self._porosity), up, un,
             _lib.ptr(self._rho) if want_macro else None,
             _lib.ptr(self._u) if want_macro else None,
-            red, self._s()))
+            red, st))
         if stencil and nsteps % 2 == 1:
             self._ul.reverse()
         self.t += int(nsteps)
