@@ -243,13 +243,6 @@ __device__ __forceinline__ void warp_aggregated_add(float* base, uint32_t node, 
   if (ok && head && v != 0.0f) atomicAdd(base + node, v);
 }
 
-// One particle per group of 8 lanes, lane r = corner r of the trilinear stencil (bit 2: +x,
-// bit 1: +y, bit 0: +z).  Each lane loads its corner's velocity and forms w_r u_r; the group's
-// first lane sums the eight products in corner order (the sequential gather of the restatement),
-// runs the particle update and hands the deposit back, and every lane deposits its own corner.
-// Eight times the threads of one-lane-per-particle keeps the SMs busy for a few ten thousand
-// particles, and the 32 deposits of a particle go out from 8 lanes at once.
-constexpr int CPL_LANES = 8;
 __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __restrict__ vel,
                               const float* __restrict__ diam, float* __restrict__ drag_old,
                               int32_t* __restrict__ active, int np, const int32_t* __restrict__ order,
@@ -258,51 +251,51 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
                               float* __restrict__ u_at) {
   const float PI_F = 3.14159265358979f;
   const uint32_t n = P.n;
-  const int lane = threadIdx.x & 31;
-  const int r = lane & (CPL_LANES - 1);
-  const int lead = lane & ~(CPL_LANES - 1);
-  // whole warps iterate together so the shuffles and the warp-level aggregation see all lanes
-  const int groups = (gridDim.x * blockDim.x) / CPL_LANES;
-  const int nloop = (np + groups - 1) / groups;
+  // whole warps iterate together so the warp-level aggregation sees converged lanes
+  const int stride = gridDim.x * blockDim.x;
+  const int nloop = (np + stride - 1) / stride;
   for (int it = 0; it < nloop; ++it) {
-    const int t = it * groups + (int)((blockIdx.x * blockDim.x + threadIdx.x) / CPL_LANES);
+    const int t = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
     const int q = t < np ? (order ? order[t] : t) : -1;
-    const bool ok = q >= 0 && active[q] != 0;
-    float x = 0, y = 0, z = 0, wr = 0;
-    uint32_t c0 = 0, node = 0;
+    bool ok = q >= 0 && active[q] != 0;
+    float x = 0, y = 0, z = 0;
+    int i = 0, j = 0, k = 0;
+    float w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float F[3] = {0, 0, 0};
+    float dep[4] = {0, 0, 0, 0};  // deposit: beta, beta * v_new
+    bool dep_ok = false;
     if (ok) {
       x = pos[q];
       y = pos[np + q];
       z = pos[2 * np + q];
-      const int i = cell_axis(x, P.nx), j = cell_axis(y, P.ny), k = cell_axis(z, P.nz);
-      const float fx = fmaxf(0.0f, fminf(1.0f, x - (float)i));
-      const float fy = fmaxf(0.0f, fminf(1.0f, y - (float)j));
-      const float fz = fmaxf(0.0f, fminf(1.0f, z - (float)k));
-      wr = ((r & 4) ? fx : (1 - fx)) * ((r & 2) ? fy : (1 - fy)) * ((r & 1) ? fz : (1 - fz));
-      const uint32_t sy = (uint32_t)P.nx, sz = (uint32_t)P.nx * (uint32_t)P.ny;
-      c0 = (uint32_t)i + sy * (uint32_t)j + sz * (uint32_t)k;
-      node = c0 + ((r & 4) ? 1u : 0u) + ((r & 2) ? sy : 0u) + ((r & 1) ? sz : 0u);
+      i = cell_axis(x, P.nx);
+      j = cell_axis(y, P.ny);
+      k = cell_axis(z, P.nz);
+      float fx = fmaxf(0.0f, fminf(1.0f, x - (float)i));
+      float fy = fmaxf(0.0f, fminf(1.0f, y - (float)j));
+      float fz = fmaxf(0.0f, fminf(1.0f, z - (float)k));
+      w[0] = (1 - fx) * (1 - fy) * (1 - fz);
+      w[1] = (1 - fx) * (1 - fy) * fz;
+      w[2] = (1 - fx) * fy * (1 - fz);
+      w[3] = (1 - fx) * fy * fz;
+      w[4] = fx * (1 - fy) * (1 - fz);
+      w[5] = fx * (1 - fy) * fz;
+      w[6] = fx * fy * (1 - fz);
+      w[7] = fx * fy * fz;
     }
-    // w_r u_r of this lane's corner, summed in corner order by the group's first lane
-    float prod[3] = {0, 0, 0};
+    const uint32_t sx = 1, sy = (uint32_t)P.nx, sz = (uint32_t)P.nx * (uint32_t)P.ny;
+    const uint32_t c0 = (uint32_t)i + sy * (uint32_t)j + sz * (uint32_t)k;
+    uint32_t nodes[8] = {c0, c0 + sz, c0 + sy, c0 + sy + sz, c0 + sx, c0 + sx + sz, c0 + sx + sy, c0 + sx + sy + sz};
     if (ok) {
+      float uf[3];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) prod[a] = wr * u[(size_t)a * n + node];
-    }
-    float uf[3];
+      for (int a = 0; a < 3; ++a) {
+        const float* v = u + (size_t)a * n;
+        float s = w[0] * v[nodes[0]];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      float sum = __shfl_sync(0xffffffffu, prod[a], lead);
-#pragma unroll
-      for (int cc = 1; cc < CPL_LANES; ++cc) {
-        const float v = __shfl_sync(0xffffffffu, prod[a], lead + cc);
-        sum = sum + v;
+        for (int cc = 1; cc < 8; ++cc) s = s + w[cc] * v[nodes[cc]];
+        uf[a] = s;
       }
-      uf[a] = sum;
-    }
-    float dep[4] = {0, 0, 0, 0};  // deposit: beta, beta * v_new
-    int dep_ok = 0;
-    if (ok && r == 0) {
       if (u_at) {
         u_at[q] = uf[0];
         u_at[np + q] = uf[1];
@@ -327,7 +320,6 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
       }
       const float gv[3] = {P.gx, P.gy, P.gz};
       const float beta = mp / (taup + P.dt);  // drag coefficient: F_new = beta (u_f - v)
-      float F[3];
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         float fnew = mp * ur[a] / (taup + P.dt);
@@ -354,11 +346,11 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
       }
       float rc = (np3[2] - P.apex) * P.tanth;
       float dx = np3[0] - P.cxf, dy = np3[1] - P.cyf;
-      float rr = sqrtf(dx * dx + dy * dy);
-      if (rr > P.margin * rc) {
-        float sc = rr > 0.0f ? (P.pullback * rc) / rr : 0.0f;
-        np3[0] = P.cxf + dx * sc;
-        np3[1] = P.cyf + dy * sc;
+      float r = sqrtf(dx * dx + dy * dy);
+      if (r > P.margin * rc) {
+        float s = r > 0.0f ? (P.pullback * rc) / r : 0.0f;
+        np3[0] = P.cxf + dx * s;
+        np3[1] = P.cyf + dy * s;
         hit = true;
       }
       if (hit) {
@@ -379,25 +371,30 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
         dep[0] = beta;
 #pragma unroll
         for (int a = 0; a < 3; ++a) dep[1 + a] = beta * nv[a];
-        dep_ok = 1;
+        dep_ok = true;
       }
     }
-    if (P.dep_cells && q >= 0 && r == 0) P.dep_cells[q] = dep_ok ? (int32_t)c0 : -1;
+    if (P.dep_cells && q >= 0) P.dep_cells[q] = dep_ok ? (int32_t)c0 : -1;
+    if (dep_ok && P.dmask) {
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) atomicOr(P.dmask + (nodes[cc] >> 5), 1u << (nodes[cc] & 31u));
+    }
     // Deposit the drag coefficient and its momentum weight (Kp += w beta, Kv += w beta v_new)
     // with the gather weights at the pre-update position; the lattice step applies the
     // particle force on the fluid, Kv - Kp u, implicitly in u.
-    dep_ok = __shfl_sync(0xffffffffu, dep_ok, lead);
-    if (dep_ok && P.dmask) atomicOr(P.dmask + (node >> 5), 1u << (node & 31u));
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      const float contrib = wr * __shfl_sync(0xffffffffu, dep[a], lead);
-      if (P.deterministic) {
-        if (dep_ok) {
-          long long fixv = __double2ll_rn((double)contrib * FIX_SCALE);
-          atomicAdd(pdrag_fix + (size_t)a * n + node, (unsigned long long)fixv);
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc) {
+        const float contrib = w[cc] * dep[a];
+        if (P.deterministic) {
+          if (dep_ok) {
+            long long fixv = __double2ll_rn((double)contrib * FIX_SCALE);
+            atomicAdd(pdrag_fix + (size_t)a * n + nodes[cc], (unsigned long long)fixv);
+          }
+        } else {
+          warp_aggregated_add(pdrag + (size_t)a * n, nodes[cc], dep_ok, contrib);
         }
-      } else {
-        warp_aggregated_add(pdrag + (size_t)a * n, node, dep_ok != 0, contrib);
       }
     }
   }
@@ -551,7 +548,7 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   P.dmask = pp->deposit_mask;
   cudaStream_t s = (cudaStream_t)stream;
   int block = 256;
-  long long want = ((long long)np * CPL_LANES + block - 1) / block;
+  long long want = ((long long)np + block - 1) / block;
   int grid = (int)(want < 152 * 16 ? want : 152 * 16);
   couple_kernel<<<grid, block, 0, s>>>(P, pos, vel, diameter, drag_old, active, np, order, u, pdrag,
                                        (unsigned long long*)pdrag_fix, u_at_particle);
