@@ -243,6 +243,23 @@ __device__ __forceinline__ void warp_aggregated_add(float* base, uint32_t node, 
   if (ok && head && v != 0.0f) atomicAdd(base + node, v);
 }
 
+__device__ __forceinline__ void warp_aggregated_or(uint32_t* base, uint32_t word, bool ok, uint32_t v) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t key = ok ? word : (0xffffffffu - (uint32_t)lane);
+  const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+  const bool head = lane == 0 || prev != key;
+  const uint32_t heads = __ballot_sync(0xffffffffu, head);
+  const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+  const uint32_t seg = (uint32_t)__popc(heads & upto);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t ss = __shfl_down_sync(0xffffffffu, seg, o);
+    uint32_t vv = __shfl_down_sync(0xffffffffu, v, o);
+    if (lane + o < 32 && ss == seg) v |= vv;
+  }
+  if (ok && head && v) atomicOr(base + word, v);
+}
+
 __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __restrict__ vel,
                               const float* __restrict__ diam, float* __restrict__ drag_old,
                               int32_t* __restrict__ active, int np, const int32_t* __restrict__ order,
@@ -375,9 +392,16 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
       }
     }
     if (P.dep_cells && q >= 0) P.dep_cells[q] = dep_ok ? (int32_t)c0 : -1;
-    if (dep_ok && P.dmask) {
+    if (P.dmask) {
+      // the x-neighbour corners (c, c + 1) mostly share a 32-cell mask word: one OR for both,
+      // aggregated over runs of lanes (cell-sorted neighbours) that hit the same word
 #pragma unroll
-      for (int cc = 0; cc < 8; ++cc) atomicOr(P.dmask + (nodes[cc] >> 5), 1u << (nodes[cc] & 31u));
+      for (int cc = 0; cc < 4; ++cc) {
+        const uint32_t a = nodes[cc], b = a + 1u;
+        const uint32_t wa = a >> 5, wb = b >> 5;
+        warp_aggregated_or(P.dmask, wa, dep_ok, (1u << (a & 31u)) | (wa == wb ? (1u << (b & 31u)) : 0u));
+        warp_aggregated_or(P.dmask, wb, dep_ok && wa != wb, 1u << (b & 31u));
+      }
     }
     // Deposit the drag coefficient and its momentum weight (Kp += w beta, Kv += w beta v_new)
     // with the gather weights at the pre-update position; the lattice step applies the
