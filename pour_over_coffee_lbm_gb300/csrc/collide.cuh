@@ -563,6 +563,22 @@ struct RedAcc<float> {
     for (int r = 0; r < POG_RED_COUNT - 1; ++r) out[r] = (double)hi[r] + (double)lo[r];
     out[POG_RED_NONFINITE] = (double)bad;
   }
+  // Sum the warp's 32 accumulators into lane 0, still in FP32 double-float form (FP64
+  // arithmetic runs at a small fraction of the FP32 rate on this GPU, so it is left to one
+  // lane per warp).
+  __device__ __forceinline__ void warp_sum() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int r = 0; r < POG_RED_COUNT - 1; ++r) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi[r], o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo[r], o);
+        two_sum(hi[r], lo[r], h2);
+        lo[r] = __fadd_rn(lo[r], l2);
+      }
+      bad += __shfl_down_sync(0xffffffffu, bad, o);
+    }
+  }
 };
 static_assert(POG_RED_NONFINITE == POG_RED_COUNT - 1, "the count slot is last");
 
@@ -587,6 +603,35 @@ __device__ __forceinline__ void block_reduce_add(double v[POG_RED_COUNT], double
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       if (lane == 0 && x != 0.0) atomicAdd(out + r, x);
+    }
+  }
+}
+
+// Block reduction of a thread's accumulator into the POG_RED_* slots (one atomic per block and
+// slot).  FP32 accumulators are summed across the warp in double-float form first and only the
+// warps' totals are converted to FP64; FP64 accumulators take block_reduce_add.
+template <typename C>
+__device__ __forceinline__ void reduce_add(RedAcc<C>& acc, double* out) {
+  if constexpr (sizeof(C) == 8) {
+    double part[POG_RED_COUNT];
+    acc.finish(part);
+    block_reduce_add(part, out);
+  } else {
+    __shared__ double sm[POG_RED_COUNT][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    acc.warp_sum();
+    if (lane == 0) {
+      double part[POG_RED_COUNT];
+      acc.finish(part);
+#pragma unroll
+      for (int r = 0; r < POG_RED_COUNT; ++r) sm[r][warp] = part[r];
+    }
+    __syncthreads();
+    if (warp == 0 && lane < POG_RED_COUNT) {
+      double x = 0.0;
+      for (int w = 0; w < nw; ++w) x += sm[lane][w];
+      if (x != 0.0) atomicAdd(out + lane, x);
     }
   }
 }

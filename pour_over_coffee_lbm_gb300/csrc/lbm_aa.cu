@@ -130,11 +130,7 @@ __global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
     aa_update<S, PARITY, REDUCE, MACRO_ONLY>(kp, f, c, fl, open, fv, force, pdrag, eps, u_prev, u_next,
                                              rho_out, u_out, acc);
   }
-  if (REDUCE) {
-    double part[POG_RED_COUNT];
-    acc.finish(part);
-    block_reduce_add(part, red);
-  }
+  if (REDUCE) reduce_add<C>(acc, red);
 }
 
 // Natural-layout copy of the AA state at parity PARITY (odd = the odd-step read gather).

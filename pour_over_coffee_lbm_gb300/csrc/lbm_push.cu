@@ -49,11 +49,7 @@ __global__ void __launch_bounds__(PUSH_BLOCK, S == POG_STORE_F64 ? 1 : 4) push_s
         St::st(fout, (uint32_t)q * n + dst, q, fv[q], rs);
     }
   }
-  if (REDUCE) {
-    double part[POG_RED_COUNT];
-    acc.finish(part);
-    block_reduce_add(part, red);
-  }
+  if (REDUCE) reduce_add<C>(acc, red);
 }
 
 template <int S, bool R>
