@@ -418,8 +418,8 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
  * particle whose deposit_cells entry (from pog_particles_couple) is >= 0: after the lattice step
  * has read the deposit, this returns pdrag to all zeros at the cost of the particles' cells
  * instead of a full-field fill.  order (nullable): the coupling pass's particle order, so that
- * neighbouring threads write neighbouring cells.  deposit_mask (nullable): cleared entirely (no
- * cell holds a deposit afterwards). */
+ * neighbouring threads write neighbouring cells.  deposit_mask (nullable): cleared entirely in
+ * the same kernel (no cell holds a deposit afterwards). */
 int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cells, int np,
                                 const int32_t* order, float* pdrag, uint32_t* deposit_mask, void* stream);
 /* pdrag[a][c] = pdrag_fix[a][c] * 2^-32, a = 0..3 (deterministic-mode conversion). */

@@ -427,8 +427,15 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
 // Zero the 8 deposit cells of each particle in all 4 components (several particles may share a
 // cell: every write is the same zero).
 __global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const int32_t* __restrict__ dep,
-                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag) {
+                                     const int32_t* __restrict__ order, int np, float* __restrict__ pdrag,
+                                     uint32_t* __restrict__ dmask) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // once the deposit is gone no cell holds one: the whole mask (n / 32 words) is cleared here too,
+  // cheaper than clearing its bits one atomic at a time and without a separate memset
+  if (dmask) {
+    const uint32_t words = (n + 31u) / 32u;
+    for (uint32_t w = (uint32_t)t; w < words; w += gridDim.x * blockDim.x) dmask[w] = 0u;
+  }
   if (t >= np) return;
   // in cell order (the coupling pass's order) neighbouring threads zero neighbouring cells
   const int32_t c = dep[order ? order[t] : t];
@@ -589,15 +596,15 @@ int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cell
   if (np == 0) return POG_OK;
   if (!deposit_cells || !pdrag) return set_error(POG_E_ARG, "NULL pointer");
   const uint32_t sy = (uint32_t)p->nx, sz = (uint32_t)p->nx * (uint32_t)p->ny;
-  clear_deposit_kernel<<<(np + 255) / 256, 256, 0, (cudaStream_t)stream>>>(sz * (uint32_t)p->nz, sy, sz,
-                                                                          deposit_cells, order, np, pdrag);
+  // a thread per particle, and at least one per 4 mask words (n / 32 words)
+  const long long words = ((long long)sz * p->nz + 31) / 32;
+  const long long pblocks = ((long long)np + 255) / 256;
+  const long long mblocks = deposit_mask ? (words + 1023) / 1024 : 0;
+  const long long want = pblocks > mblocks ? pblocks : mblocks;
+  clear_deposit_kernel<<<(int)want, 256, 0, (cudaStream_t)stream>>>(sz * (uint32_t)p->nz, sy, sz, deposit_cells,
+                                                                   order, np, pdrag, deposit_mask);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
-  // once the deposit is gone no cell holds one: clearing the whole mask (ncell / 8 bytes) is
-  // cheaper than clearing its bits one atomic at a time
-  if (deposit_mask)
-    POG_TRY_CUDA(cudaMemsetAsync(deposit_mask, 0, (((size_t)sz * (uint32_t)p->nz + 31) / 32) * sizeof(uint32_t),
-                                 (cudaStream_t)stream));
   return POG_OK;
 }
 
