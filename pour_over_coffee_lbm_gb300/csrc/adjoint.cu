@@ -22,13 +22,6 @@ namespace pog {
 
 constexpr int ADJ_BLOCK = 256;
 
-template <typename C>
-__device__ __forceinline__ void eq_all(C rho, C ux, C uy, C uz, C feq[19]) {
-  const C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
-#pragma unroll
-  for (int q = 0; q < 19; ++q) feq[q] = feq_q<C>(q, rho, ux, uy, uz, usq15);
-}
-
 // d(sum_q lam_q feq_q)/d(rho, u) for feq at (rho, u): returns bar_rho, bar_u.
 template <typename C>
 __device__ __forceinline__ void eq_vjp(const C lam[19], C rho, C ux, C uy, C uz, C& brho, C& bux,
@@ -71,18 +64,6 @@ __device__ __forceinline__ void eq_vjp_diff(const C a[19], const C b[19], C rho,
   bux = bx;
   buy = by;
   buz = bz;
-}
-
-template <typename C>
-__device__ __forceinline__ C chebyshev_T(int k, C s) {
-  C t0 = (C)1, t1 = s;
-  if (k == 0) return t0;
-  for (int i = 2; i <= k; ++i) {
-    C t2 = (C)2 * s * t1 - t0;
-    t0 = t1;
-    t1 = t2;
-  }
-  return t1;
 }
 
 // Inlet cell c (f* = feq(rho, (0, 0, u_z(a)))): bar f (all directions equal) from the pulled
