@@ -225,8 +225,10 @@ __device__ __forceinline__ bool pour_impact(const float* b, float x, float y, fl
 // Segmented warp sum over runs of consecutive lanes that share `node` (in cell order equal
 // nodes are consecutive; in any other order a repeated node simply starts a new run).  Runs
 // are numbered from the head-flag ballot, the suffix sum stays inside a run, and the head lane
-// of each run adds the run's total with one atomic.
-__device__ __forceinline__ void warp_aggregated_add(float* base, uint32_t node, bool ok, float v) {
+// of each run adds the run's total with one atomic per component.  The four deposit components
+// of a node share the runs and ride the same shuffles.
+__device__ __forceinline__ void warp_aggregated_add4(float* base, uint32_t n, uint32_t node, bool ok, float v0,
+                                                     float v1, float v2, float v3) {
   const int lane = threadIdx.x & 31;
   const uint32_t key = ok ? node : (0xffffffffu - (uint32_t)lane);
   const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
@@ -236,11 +238,22 @@ __device__ __forceinline__ void warp_aggregated_add(float* base, uint32_t node, 
   const uint32_t seg = (uint32_t)__popc(heads & upto);
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t ss = __shfl_down_sync(0xffffffffu, seg, o);
-    float vv = __shfl_down_sync(0xffffffffu, v, o);
-    if (lane + o < 32 && ss == seg) v += vv;
+    const uint32_t ss = __shfl_down_sync(0xffffffffu, seg, o);
+    const float a0 = __shfl_down_sync(0xffffffffu, v0, o), a1 = __shfl_down_sync(0xffffffffu, v1, o);
+    const float a2 = __shfl_down_sync(0xffffffffu, v2, o), a3 = __shfl_down_sync(0xffffffffu, v3, o);
+    if (lane + o < 32 && ss == seg) {
+      v0 += a0;
+      v1 += a1;
+      v2 += a2;
+      v3 += a3;
+    }
   }
-  if (ok && head && v != 0.0f) atomicAdd(base + node, v);
+  if (ok && head) {
+    if (v0 != 0.0f) atomicAdd(base + node, v0);
+    if (v1 != 0.0f) atomicAdd(base + n + node, v1);
+    if (v2 != 0.0f) atomicAdd(base + 2u * n + node, v2);
+    if (v3 != 0.0f) atomicAdd(base + 3u * n + node, v3);
+  }
 }
 
 __device__ __forceinline__ void warp_aggregated_or(uint32_t* base, uint32_t word, bool ok, uint32_t v) {
@@ -406,20 +419,23 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
     // Deposit the drag coefficient and its momentum weight (Kp += w beta, Kv += w beta v_new)
     // with the gather weights at the pre-update position; the lattice step applies the
     // particle force on the fluid, Kv - Kp u, implicitly in u.
+    if (P.deterministic) {
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
+      for (int a = 0; a < 4; ++a) {
 #pragma unroll
-      for (int cc = 0; cc < 8; ++cc) {
-        const float contrib = w[cc] * dep[a];
-        if (P.deterministic) {
+        for (int cc = 0; cc < 8; ++cc) {
+          const float contrib = w[cc] * dep[a];
           if (dep_ok) {
             long long fixv = __double2ll_rn((double)contrib * FIX_SCALE);
             atomicAdd(pdrag_fix + (size_t)a * n + nodes[cc], (unsigned long long)fixv);
           }
-        } else {
-          warp_aggregated_add(pdrag + (size_t)a * n, nodes[cc], dep_ok, contrib);
         }
       }
+    } else {
+#pragma unroll
+      for (int cc = 0; cc < 8; ++cc)
+        warp_aggregated_add4(pdrag, n, nodes[cc], dep_ok, w[cc] * dep[0], w[cc] * dep[1], w[cc] * dep[2],
+                             w[cc] * dep[3]);
     }
   }
 }
