@@ -294,9 +294,11 @@ def plugin_rows(cfg, pc, steps, peak):
 
     def row(name, fn, nbytes):
         us = _time_launches(fn, 20) * 1e6
-        gbs = nbytes / (us * 1e-6) / 1e9
-        rows[name] = {"kernel_us": round(us, 2), "algorithmic_bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
-                      "frac": round(gbs / peak[0], 4)}
+        rows[name] = {"kernel_us": round(us, 2)}
+        if nbytes:
+            gbs = nbytes / (us * 1e-6) / 1e9
+            rows[name].update({"algorithmic_bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
+                               "frac": round(gbs / peak[0], 4)})
 
     row("pog_phase_normals", mp.compute_gradients, inner * (4 + 16))
     row("pog_phase_surface_tension", lambda: mp._tension(True, outputs=False),
@@ -304,6 +306,18 @@ def plugin_rows(cfg, pc, steps, peak):
     row("pog_phase_update", mp.update_phase_field_cahn_hilliard, n * (4 + 4 + 12 + 4 + 4 + 4) + inner * 4)
     row("pog_pressure_force", lambda: drive._accumulate(1.0), n * (4 + 4 + 24))
     row("pog_filter_update", fs.update_dynamic_resistance, n * 4 + n_por * 16)
+    row("pog_filter_particles", lambda: fs.block_particles_at_filter(ps), pc.count * (4 + 12 + 12))
+    row("pog_phase_properties", mp.update_density_from_phase, n * (4 + 4 + 4))
+    row("pog_pour_phase", lambda: pour.apply_gradual_phase_change(mp), 0)
+    # diagnostics: one pass over rho, u and the previous check's rho, u
+    rho_prev, u_prev = s._rho.clone(), s._u.clone()
+    st = torch.empty(24, dtype=torch.float64, device="cuda")
+    zp = torch.empty(cfg.nz, dtype=torch.float64, device="cuda")
+
+    def stats():
+        _lib.check(lib.pog_field_stats(s._p, s._rho.data_ptr(), s._u.data_ptr(), rho_prev.data_ptr(),
+                                       u_prev.data_ptr(), st.data_ptr(), zp.data_ptr(), _lib.stream_handle()))
+    row("pog_field_stats", stats, n * 32)
     out = {"workload": "%dx%dx%d production step: pour stream + phase change, pressure drive (force, cap 1e-5), "
                        "surface tension (sigma 1e-5), FP32 lattice step reading the phase field, filter paper "
                        "(%d particles), phase-field step" % (cfg.nx, cfg.ny, cfg.nz, pc.count),
@@ -313,7 +327,9 @@ def plugin_rows(cfg, pc, steps, peak):
            "note": "algorithmic bytes: normals 4 B read + 16 B written per interior cell; surface tension "
                    "4 B per interior cell + 4 B per cell with a gradient + 44 B per interface cell; phase "
                    "update 28 B per cell + 4 B mu per interior cell; pressure force 32 B per cell; "
-                   "filter update 4 B per cell + 16 B per paper cell"}
+                   "filter update 4 B per cell + 16 B per paper cell; filter particles 28 B per particle; "
+                   "phase properties 12 B per cell; field stats 32 B per cell; pour phase: the stream's "
+                   "planes only (time alone)"}
     del s, ps, mp, pour, drive, fs
     torch.cuda.empty_cache()
     return out
