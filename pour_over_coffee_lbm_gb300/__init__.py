@@ -19,7 +19,8 @@ __all__ = [
     "LatticeConfig", "ParticleConfig", "GB300LBMSolver", "UnifiedLBMSolver",
     "create_unified_solver", "CoffeeParticleSystem", "OutflowAdjoint", "outflow_loss",
     "LBMSolverProtocol", "ParticleCoupledLBMProtocol", "validate_lbm_solver",
-    "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter", "FilterPaperSystem",
+    "PrecisePouringSystem", "SlabLattice", "LBMDiagnostics", "SnapshotWriter", "export_data_for_analysis",
+    "FilterPaperSystem",
     "PressureGradientDrive", "MultiphaseFlow3D",
 ]
 
@@ -39,7 +40,7 @@ def __getattr__(name):
     if name == "PrecisePouringSystem":
         from .pouring import PrecisePouringSystem
         return PrecisePouringSystem
-    if name in ("LBMDiagnostics", "SnapshotWriter"):
+    if name in ("LBMDiagnostics", "SnapshotWriter", "export_data_for_analysis"):
         from . import diagnostics
         return getattr(diagnostics, name)
     if name == "MultiphaseFlow3D":

@@ -254,6 +254,69 @@ class SnapshotWriter:
             self._thread = None
 
 
+# Physical scales of the reference's config, used only for the export's metadata
+# (config/core.py:59-81: 14 cm over 224 planes, 0.01 lu/ts, time factor 1.2;
+# config/physics.py:42,69,107-111: V60 height, 2 cm/s, water at 90 C).
+EXPORT_SCALES = {"scale_length": 0.14 / 224, "scale_velocity": 0.01, "time_factor": 1.2,
+                 "l_char": 0.085, "u_char": 0.02, "nu_char": 3.15e-7}
+
+
+def export_data_for_analysis(lbm, simulation_time, step_num, particles=None, filter_system=None,
+                             out_dir: str = ".", scales: Optional[dict] = None) -> list:
+    """The reference's analysis export (src/visualization/enhanced_visualizer.py:1487-1560):
+    `cfd_data_export_step_NNNN.json` with the velocity, density and pressure fields (ρ c_s^2),
+    the active particles, the filter statistics and the run's metadata, and
+    `cfd_data_export_step_NNNN.npz` with the entries that are arrays (density and pressure, float64,
+    indexed (NX, NY, NZ)).  The Reynolds number of the metadata follows
+    calculate_flow_characteristics (:450-471): mean physical |u| over |u| > 1e-6 m/s (u_char when
+    none) times l_char over nu_char.  Returns the two paths, or [] after a failure, which is
+    printed, as the reference does."""
+    import json
+    sc = dict(EXPORT_SCALES, **(scales or {}))
+    try:
+        export = {}
+        if hasattr(lbm, "u") and hasattr(lbm, "rho"):
+            u = lbm.u.to_numpy()
+            rho = lbm.rho.to_numpy()
+            export["velocity_field"] = {"u_x": u[..., 0].tolist(), "u_y": u[..., 1].tolist(),
+                                        "u_z": u[..., 2].tolist(),
+                                        "magnitude": np.sqrt(np.sum(u ** 2, axis=3)).tolist()}
+            export["density_field"] = rho.tolist()
+            export["pressure_field"] = (rho * (1.0 / 3.0)).tolist()
+            umag = np.sqrt(u[..., 0] ** 2 + u[..., 1] ** 2 + u[..., 2] ** 2) * sc["scale_velocity"]
+            act = umag[umag > 1e-6]
+            uc = float(np.mean(act)) if act.size else sc["u_char"]
+            reynolds = uc * sc["l_char"] / sc["nu_char"] if uc > 0 and sc["nu_char"] > 0 else 0.0
+        else:
+            reynolds = 0
+        if particles is not None:
+            pos = particles.position.to_numpy()
+            vel = particles.velocity.to_numpy()
+            active = particles.active.to_numpy()
+            export["particles"] = {"positions": pos[active == 1].tolist(),
+                                   "velocities": vel[active == 1].tolist(),
+                                   "count": int(np.sum(active))}
+        if filter_system is not None:
+            export["filter"] = filter_system.get_filter_statistics()
+        nx, ny, nz = (int(lbm.NX), int(lbm.NY), int(lbm.NZ))
+        export["metadata"] = {"simulation_time": simulation_time, "step_number": step_num,
+                              "grid_size": [nx, ny, nz],
+                              "physical_parameters": {
+                                  "scale_length": sc["scale_length"],
+                                  "scale_time": sc["scale_length"] / sc["scale_velocity"] * sc["time_factor"],
+                                  "reynolds_number": float(reynolds)}}
+        base = os.path.join(out_dir, "cfd_data_export_step_%04d" % step_num)
+        json_file, numpy_file = base + ".json", base + ".npz"
+        with open(json_file, "w") as f:
+            json.dump(export, f, indent=2)
+        np.savez_compressed(numpy_file, **{k: np.array(v) for k, v in export.items()
+                                           if isinstance(v, (list, np.ndarray))})
+        return [json_file, numpy_file]
+    except Exception as e:  # the reference reports and carries on
+        print("data export failed: %s" % e)
+        return []
+
+
 def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=None, multiphase=None) -> None:
     """Everything a run needs to continue bit for bit: the raw distribution buffer in its
     storage format, time index, flags, porosity, explicit force, LES velocity buffers, the phase

@@ -18,8 +18,11 @@ from pour_over_coffee_lbm_gb300.params import LatticeConfig, ParticleConfig
 pytestmark = pytest.mark.gpu
 
 
-def test_field_stats_match_numpy(cuda):
-    cfg = LatticeConfig(nx=40, ny=36, nz=44)
+# one cell per thread; runs of several steps whose plane boundaries fall inside a 32-cell step;
+# planes of 20 cells (several boundaries per step); long runs (about 1,100 cells per warp)
+@pytest.mark.parametrize("shape", [(40, 36, 44), (100, 60, 50), (5, 4, 3000), (256, 256, 64)])
+def test_field_stats_match_numpy(cuda, shape):
+    cfg = LatticeConfig(nx=shape[0], ny=shape[1], nz=shape[2])
     rng = np.random.default_rng(3)
     shape = (cfg.nz, cfg.ny, cfg.nx)
     rho = (1.0 + 0.01 * rng.normal(size=shape)).astype(np.float32)
@@ -104,6 +107,17 @@ def test_snapshot_files(cuda, tmp_path):
     assert rho.shape == (24, 28, 32) and np.array_equal(rho, s.rho.to_numpy())
     ref = np.sqrt((s.u.to_numpy().astype(np.float32) ** 2).sum(-1))
     assert np.allclose(umag, ref, rtol=1e-6, atol=1e-9)
+
+
+def test_export_data_for_analysis(cuda, tmp_path):
+    from pour_over_coffee_lbm_gb300.diagnostics import export_data_for_analysis
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    s = GB300LBMSolver(LatticeConfig(nx=12, ny=10, nz=14))
+    s.run(5, want_macro=True)
+    out = export_data_for_analysis(s, 5.0, 5, out_dir=str(tmp_path))
+    assert len(out) == 2
+    z = np.load(out[1])
+    assert np.array_equal(z["density_field"], s.rho.to_numpy().astype(np.float64))
 
 
 def test_checkpoint_resume_is_bit_identical(cuda, tmp_path):
