@@ -7,7 +7,9 @@ The reference computes every statistic with numpy on full `to_numpy()` copies of
 field transfers per check, plus a host copy of both as `prev`).  Here pog_field_stats reduces
 rho and u on the device to POG_STAT_COUNT doubles and the per-plane density profile; `prev` stays
 on the device; only the small vectors come back.  Method names and dict keys follow the
-reference so callers read the same reports; lengths and times are in lattice units.
+reference so callers read the same reports.  Lengths, velocities and times are in lattice units
+unless `scale_length`, `scale_velocity` and `dt` are set to the reference's config scales, which
+reproduce its physical-unit reports.
 """
 import math
 import os
@@ -52,7 +54,12 @@ class LBMDiagnostics:
         self.initial_mass = 0.0
         self.accumulated_inflow = 0.0
         self.reference_density = 1.0
+        # lattice units by default; the reference's config.DT, SCALE_LENGTH and SCALE_VELOCITY
+        # (1.0, 0.000625 m, 0.01) reproduce its reports in physical units
         self.dt = 1.0
+        self.scale_length = 1.0
+        self.scale_velocity = 1.0
+        self.prev_phi = None  # device copy of the phase field at the previous check
         self.calculation_times = {"light": [], "medium": [], "heavy": []}
         self._stats = None
         self._zp = None
@@ -87,7 +94,7 @@ class LBMDiagnostics:
         if medium:
             t0 = time.time()
             d["conservation"] = self.check_conservation_laws(refresh=False)
-            d["multiphase"] = {"status": "no_multiphase"}
+            d["multiphase"] = self.analyze_multiphase_quality()
             self.calculation_times["medium"].append(time.time() - t0)
         if heavy:
             t0 = time.time()
@@ -169,13 +176,75 @@ class LBMDiagnostics:
         st = self._s(refresh)
         plane_mean = self._zp / float(self.lbm.NX * self.lbm.NY)
         wet = np.where(plane_mean > self.reference_density + 0.1)[0]
-        phys = {"wetting_front_position": float(wet.max()) if wet.size else 0.0,
-                "system_water_volume": max(0.0, st[STAT_MASS] - self.reference_density * self.lbm.n),
-                "inlet_flow_rate": (self.pouring.get_current_flow_rate() if self.pouring is not None else 0.0),
-                "outlet_flow_rate": float(self.lbm.last_outflow)}
+        L = self.scale_length
+        inlet = 0.0
+        if self.pouring is not None and hasattr(self.pouring, "get_current_flow_rate"):
+            inlet = float(self.pouring.get_current_flow_rate())
+        phys = {"wetting_front_position": float(wet.max()) * L if wet.size else 0.0,
+                "system_water_volume": max(0.0, (st[STAT_MASS] - self.reference_density * self.lbm.n) * L ** 3),
+                "inlet_flow_rate": inlet, "outlet_flow_rate": self._estimate_outlet_flow()}
         if self.particles is not None:
-            phys["particle_dynamics"] = self.particles.get_coupling_diagnostics()
+            phys["particle_dynamics"] = self._analyze_coffee_bed_dynamics()
         return phys
+
+    def _estimate_outlet_flow(self) -> float:
+        """lbm_diagnostics.py:439-452: the downward z velocity summed over the five bottom planes,
+        times scale_velocity * scale_length^2; reduced on the device."""
+        uz = self.lbm._u[2, :5]
+        down = torch.clamp(-uz, min=0.0).double().sum().item()
+        return float(down * self.scale_velocity * self.scale_length ** 2)
+
+    def _analyze_coffee_bed_dynamics(self) -> dict:
+        """lbm_diagnostics.py:409-437: height and radial spread of the active particles (the
+        reference's numpy arithmetic on host copies of the particle arrays)."""
+        p = self.particles
+        if not hasattr(p, "position") or not hasattr(p, "active"):
+            return {"status": "no_particle_data"}
+        pos = p.position.to_numpy()
+        act = p.active.to_numpy()
+        ap = pos[act == 1]
+        if len(ap) == 0:
+            return {"status": "no_active_particles"}
+        L = self.scale_length
+        z = ap[:, 2]
+        d = {"active_particle_count": len(ap), "bed_height_mean": float(np.mean(z) * L),
+             "bed_height_std": float(np.std(z) * L),
+             "bed_height_range": [float(np.min(z) * L), float(np.max(z) * L)]}
+        cx, cy = self.lbm.NX * 0.5, self.lbm.NY * 0.5
+        r = np.sqrt((ap[:, 0] - cx) ** 2 + (ap[:, 1] - cy) ** 2)
+        d["radial_distribution_mean"] = float(np.mean(r) * L)
+        d["radial_distribution_std"] = float(np.std(r) * L)
+        return d
+
+    def _phi(self) -> Optional[torch.Tensor]:
+        """The multiphase object's phase field as a device tensor (a tensor, a FieldView, or any
+        field with to_numpy)."""
+        phi = getattr(self.multiphase, "phi", None) if self.multiphase is not None else None
+        if phi is None:
+            return None
+        if isinstance(phi, torch.Tensor):
+            return phi
+        t = getattr(phi, "tensor", None)
+        if isinstance(t, torch.Tensor):
+            return t
+        return torch.as_tensor(np.asarray(phi.to_numpy()), device=self.lbm.device)
+
+    def analyze_multiphase_quality(self) -> dict:
+        """lbm_diagnostics.py:293-326: interface cells (0.1 < phi < 0.9), water fraction and the
+        change of phi since the previous check, reduced on the device."""
+        phi = self._phi()
+        if phi is None:
+            return {"status": "no_multiphase"}
+        a = {"interface_thickness": int(((phi > 0.1) & (phi < 0.9)).sum().item()),
+             "water_fraction": float(phi.double().mean().item())}
+        if self.prev_phi is not None:
+            change = torch.linalg.vector_norm((phi - self.prev_phi).double()).item()
+            a["phase_change_rate"] = float(change / self.dt)
+        else:
+            a["phase_change_rate"] = 0.0
+        r = a["phase_change_rate"]
+        a["phase_stability_grade"] = "Excellent" if r < 1e-6 else ("Good" if r < 1e-4 else "Dynamic")
+        return a
 
     def detailed_flow_analysis(self, refresh: bool = True) -> dict:
         """lbm_diagnostics.py:372-407: |u| statistics, per-component spread, region means."""
@@ -200,6 +269,12 @@ class LBMDiagnostics:
         else:
             self.prev[0].copy_(self.lbm._rho)
             self.prev[1].copy_(self.lbm._u)
+        phi = self._phi()
+        if phi is not None:
+            if self.prev_phi is None or self.prev_phi.shape != phi.shape:
+                self.prev_phi = phi.clone()
+            else:
+                self.prev_phi.copy_(phi)
 
     def get_performance_stats(self) -> dict:
         out = {}

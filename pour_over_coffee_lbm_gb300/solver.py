@@ -182,7 +182,6 @@ class GB300LBMSolver:
         self.use_les = c.les_mode != LES_OFF
         self.boundary_manager = _FusedBoundaryManager()
         self.opposite_dir = OPPOSITE.copy()
-        self.last_outflow = 0.0
         self._timing = {"steps": 0, "seconds": 0.0}
         self.initialize_fields(c.rho0, (0.0, 0.0, 0.0))
 

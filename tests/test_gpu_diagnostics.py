@@ -94,6 +94,31 @@ def test_diagnostics_reports_match_reference_formulas(cuda):
     assert "wetting_front_position" in d1["v60_physics"]
 
 
+def test_reports_match_the_reference_diagnostics(cuda):
+    """The reference's LBMDiagnostics run on the same fields (tests/golden/diag_reference.*,
+    made by tests/golden/make_diag_golden.py from its own code): every report of both checks,
+    to the reference's float32 precision, with a phase field, particles and a pour flow rate."""
+    from diag_golden import Field, Holder, Pour, compare, load
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    z, meta = load()
+    nx, ny, nz = meta["shape"]
+    s = GB300LBMSolver(LatticeConfig(nx=nx, ny=ny, nz=nz, gravity=(0.0, 0.0, -meta["gravity_lu"])))
+    mp, ps = Holder(), Holder()
+    ps.position, ps.active = Field(z["position"]), Field(z["active"])
+    diag = LBMDiagnostics(s, multiphase=mp, particles=ps, pouring=Pour(meta["flow_rate"]))
+    diag.dt, diag.scale_length, diag.scale_velocity = meta["dt"], meta["scale_length"], meta["scale_velocity"]
+    ours = []
+    for step, tag in ((0, "a"), (100, "b")):
+        # the fields as the solver's moments, (NX, NY, NZ[, 3]) -> device (NZ, NY, NX) / (3, NZ, NY, NX)
+        s._rho.copy_(torch.as_tensor(z["rho_" + tag].transpose(2, 1, 0).copy()))
+        s._u.copy_(torch.as_tensor(z["u_" + tag].transpose(3, 2, 1, 0).copy()))
+        s._macro_dirty = s._u_stale = False
+        mp.phi = torch.as_tensor(z["phi_" + tag].transpose(2, 1, 0).copy()).cuda()
+        ours.append(diag.update_diagnostics(step, float(step), force_update=True))
+    for o, r in zip(ours, meta["reports"]):
+        compare(o, r, loose=("mass_conservation_error", "total_mass", "initial_mass"))
+
+
 def test_snapshot_files(cuda, tmp_path):
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     s = GB300LBMSolver(LatticeConfig(nx=24, ny=28, nz=32))
