@@ -499,7 +499,6 @@ def precision_line(storage, steps, peak, case="les_band"):
     for _ in range(4):
         s.run(1)
     torch.cuda.synchronize()
-    import pour_over_coffee_lbm_gb300._lib as L
     t0 = s.t
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):

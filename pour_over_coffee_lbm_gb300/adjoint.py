@@ -13,11 +13,10 @@ The reference has no differentiable path (no Taichi autodiff on it); this is new
 import dataclasses
 from typing import Optional
 
-import numpy as np
 import torch
 
 from . import _lib
-from .params import (CELL_POROUS, INLET_NCOEF, RED_COUNT, RED_OUTFLOW, STORE_F32, STORE_F64,
+from .params import (INLET_NCOEF, RED_COUNT, RED_OUTFLOW, STORE_F32, STORE_F64,
                      LatticeConfig)
 
 _DT = {STORE_F32: torch.float32, STORE_F64: torch.float64}

@@ -7,7 +7,6 @@ NX, NY, NZ, TAU_WATER, SMAGORINSKY_CONSTANT ...); `from_reference_config` maps a
 import ctypes
 import dataclasses
 import math
-from typing import Optional
 
 import numpy as np
 

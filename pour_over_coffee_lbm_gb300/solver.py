@@ -6,8 +6,6 @@ LBMSolverProtocol and ParticleCoupledLBMProtocol (src/core/lbm_protocol.py).  De
 lives in torch CUDA tensors; every step is one fused libpog kernel launch.  There is no CPU
 path: without a GPU and the library, construction raises.
 """
-import struct
-import time
 from typing import Any, Optional, Tuple
 
 import numpy as np
@@ -15,8 +13,7 @@ import torch
 
 from . import _lib
 from .params import (CELL_INLET, CELL_NEAR_SOLID, CELL_OUTLET, CELL_POROUS, CELL_SOLID,
-                     LES_LOCAL, LES_OFF, LES_STENCIL, RED_COUNT, RED_MASS, RED_MOMX,
-                     RED_NONFINITE, RED_OUTFLOW, STORE_BF16S, STORE_F16S, STORE_F32, STORE_F64,
+                     LES_LOCAL, LES_OFF, LES_STENCIL, RED_COUNT, STORE_BF16S, STORE_F16S, STORE_F32, STORE_F64,
                      LatticeConfig)
 
 OPPOSITE = np.array([0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15], dtype=np.int32)
