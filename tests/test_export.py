@@ -86,3 +86,29 @@ def test_export_at_rest_uses_the_characteristic_velocity(tmp_path):
 def test_export_failure_returns_empty(tmp_path):
     rho, u = _case()
     assert export_data_for_analysis(_Lattice(rho, u), 0.0, 1, out_dir=str(tmp_path / "missing")) == []
+
+
+def test_export_matches_the_reference_export(tmp_path):
+    """The reference's own EnhancedVisualizer.export_data_for_analysis on the same inputs
+    (tests/golden/export_reference.*, made by tests/golden/make_export_golden.py): file names,
+    the JSON document and the .npz arrays, identical."""
+    import os
+    root = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    ref = json.load(open(os.path.join(root, "export_reference.json")))
+    z = np.load(os.path.join(root, "export_reference.npz"))
+    lat = _Lattice(z["rho"], z["u"])
+    ps = _Particles(z["position"], z["velocity"], z["active"])
+
+    class _RefFilter:
+        def get_filter_statistics(self):
+            return {"total_filter_nodes": 3, "average_resistance": 0.5, "average_blockage": 1.25,
+                    "average_flow_rate": 0.002, "max_blockage": 4.0}
+
+    out = export_data_for_analysis(lat, ref["simulation_time"], ref["step"], particles=ps,
+                                   filter_system=_RefFilter(), out_dir=str(tmp_path))
+    assert [p.split("/")[-1] for p in out] == ref["files"]
+    assert json.load(open(out[0])) == ref["json"]
+    ours = np.load(out[1])
+    assert sorted(ours.files) == sorted(k[4:] for k in z.files if k.startswith("npz_"))
+    for k in ours.files:
+        assert ours[k].dtype == z["npz_" + k].dtype and np.array_equal(ours[k], z["npz_" + k]), k
