@@ -98,3 +98,71 @@ def test_particle_impact_matches_reference():
         m = rho_p * math.pi / 6 * float(d[p]) ** 3
         assert np.allclose(dv[:, p], F / m * pc.dt, rtol=1e-4, atol=1e-7), p
     assert np.abs(dv[:, 0]).max() > 0 and np.abs(dv[:, 1]).max() > 0 and np.abs(dv[:, 2]).max() == 0
+
+
+# ---- against the reference's own kernels (tests/golden/pour_reference.npz, made by
+# tests/golden/make_pour_golden.py, which runs precise_pouring.py's kernel source in float32) ----
+def _ref():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "pour_reference.npz"))
+
+
+def _ref_block(z, x, y, flow, dt, pattern=0):
+    return _block(float(x), float(y), pattern=pattern, flow=flow, dt=dt, velocity=float(z["velocity"]),
+                  ztop=float(z["ztop"]), diameter=float(z["diameter"]))
+
+
+def test_pour_force_matches_reference_kernel():
+    z = _ref()
+    cfg = LatticeConfig(nx=24, ny=24, nz=24, storage=STORE_F64, band_thickness=0.0, u_inlet=0.0)
+    flags = orc.build_flags(cfg)
+    f = orc.init_equilibrium(cfg, flags, np.float64)
+    b = _ref_block(z, *z["force_pos"], flow=1.3, dt=0.5)
+    _, rho, u = orc.step(cfg, flags, f, pour=b)
+    a = rho * cfg.gravity[2] - 2.0 * rho * u[2]  # the pour acceleration at rest (see above)
+    ref = -z["force"][..., 2].transpose(2, 1, 0).astype(np.float64)  # (NX,NY,NZ) -> (NZ,NY,NX)
+    fluid = (flags & 0x7) == 0
+    assert np.count_nonzero(ref[fluid]) > 50
+    assert np.allclose(a[fluid], ref[fluid], rtol=2e-6, atol=1e-9)
+
+
+def test_spiral_trajectory_matches_reference_kernel():
+    z = _ref()
+    cfg = LatticeConfig(nx=64, ny=64, nz=24)
+    b = _ref_block(z, 32.0, 30.0, flow=1.0, dt=0.9, pattern=1)
+    b[POUR_SPIRAL_SPEED] = 1.0  # start_pouring's spiral speed
+    for step, (x, y) in enumerate(z["trajectory"]):
+        orc.pour_advance(cfg, b)
+        assert abs(b[POUR_X] - x) < 2e-4 and abs(b[POUR_Y] - y) < 2e-4, (step, b[POUR_X], b[POUR_Y], x, y)
+
+
+def test_pour_phase_matches_reference_kernel():
+    z = _ref()
+    cfg = LatticeConfig(nx=24, ny=24, nz=24, band_thickness=0.0)
+    flags = np.zeros((24, 24, 24), np.uint32)  # the reference case has no solid cells
+    phi = np.ascontiguousarray(z["phase_in"].transpose(2, 1, 0))
+    b = _ref_block(z, 12.0, 11.0, flow=1.3, dt=0.5)
+    orc.pour_phase(cfg, flags, phi, 0.5, b)
+    ref = z["phase_out"].transpose(2, 1, 0)
+    assert np.count_nonzero(ref != z["phase_in"].transpose(2, 1, 0)) > 100
+    assert np.allclose(phi, ref, rtol=0, atol=2e-6)
+
+
+def test_particle_impact_matches_reference_kernel():
+    z = _ref()
+    cfg = LatticeConfig(nx=24, ny=24, nz=24, band_thickness=0.0)
+    pc = ParticleConfig(count=3, deterministic=True)
+    b = _ref_block(z, 12.0, 12.0, flow=1.3, dt=1.0)
+    b[POUR_IMPACT], b[POUR_IMPACT_MAX], b[POUR_IMPACT_ZMIN] = 10.0 * b[POUR_FLOW], 0.05, 0.3 * 24
+    pos = np.ascontiguousarray(z["impact_pos"].T)
+    vel = np.zeros((3, 3), np.float32)
+    d = np.array([0.6, 0.7, 0.8], np.float32)
+    act = np.ones(3, np.int32)
+    u = np.zeros((3, 24, 24, 24), np.float32)
+    a = orc.particles_couple(cfg, pc, pos, vel, d, np.zeros((3, 3), np.float32), act, u, pour=b)
+    n = orc.particles_couple(cfg, pc, pos, vel, d, np.zeros((3, 3), np.float32), act, u)
+    dv = (a[1] - n[1]).astype(np.float64)
+    m = pc.density_ratio * cfg.rho0 * math.pi / 6 * d.astype(np.float64) ** 3
+    F = dv * m / pc.dt  # the impact force each particle received
+    assert np.abs(z["impact_force"]).max() > 0
+    assert np.allclose(F, z["impact_force"].T, rtol=1e-4, atol=1e-8)
