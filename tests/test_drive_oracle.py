@@ -86,3 +86,36 @@ def test_density_drive_matches_reference():
         ref = np.where(flags & CELL_SOLID, ref, new).astype(f32)
         orc.density_drive(cfg, flags, rho, target, 0.025, 0.001, 0.5, 2.0)
     assert np.array_equal(rho, ref)
+
+
+# ---- against the reference's own kernels (tests/golden/drive_reference.npz, made by
+# tests/golden/make_drive_golden.py, which runs pressure_gradient_drive.py's kernel source) ----
+def _ref():
+    import os
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "drive_reference.npz"))
+
+
+def _zyx(a):
+    """(NX, NY, NZ[, 3]) of the reference -> (NZ, NY, NX) / (3, NZ, NY, NX)."""
+    return np.ascontiguousarray(a.transpose(2, 1, 0) if a.ndim == 3 else a.transpose(3, 2, 1, 0))
+
+
+def test_drive_matches_reference_kernels():
+    z = _ref()
+    nx, ny, nz = z["rho"].shape
+    cfg = LatticeConfig(nx=nx, ny=ny, nz=nz)
+    flags = _zyx(z["solid"]).astype(np.uint32) * np.uint32(CELL_SOLID)
+    rho = _zyx(z["rho"])
+    for case, scale, cap, base in (("force", 1.0, 0.12, None), ("capped", 1.0, 0.002, None),
+                                   ("mixed", 0.5, 0.12, "base")):
+        F = _zyx(z[base]) if base else np.zeros((3, nz, ny, nx), f32)
+        orc.pressure_force(cfg, flags, rho, F, scale, cap)
+        assert np.array_equal(F, _zyx(z[case + "_force"])), case
+    # the density drive: a per-plane target (the reference's target field is uniform in x, y)
+    t = z["target"]
+    assert np.array_equal(t, np.broadcast_to(t[:1, :1, :], t.shape))
+    r = rho.copy()
+    for _ in range(3):
+        orc.density_drive(cfg, flags, r, np.ascontiguousarray(t[0, 0, :]), 0.025, 0.001, 0.5, 2.0)
+    assert np.array_equal(r, _zyx(z["density_rho"]))
+    assert np.count_nonzero(r != rho) > 1000
