@@ -7,8 +7,8 @@ Semantics: a `ti.kernel` or `ti.func` runs as the plain Python function it decor
 `ti.ndrange` is a nested range.  Fields are NumPy arrays of their dtype (f32 -> float32,
 i32 -> int32), so scalar arithmetic on field values stays in float32 as it does in Taichi (NumPy's
 promotion keeps float32 against Python scalars).  Vectors are float32 NumPy arrays with .x/.y/.z,
-.norm() and .dot().  Parallel-for atomics, struct-for over fields, SNodes and autodiff are not
-provided: a generator that reaches them fails loudly.
+.norm() and .dot().  `ti.random()` returns 0.5.  Parallel-for atomics, struct-for over fields,
+SNodes and autodiff are not provided: a generator that reaches them fails loudly.
 """
 import itertools
 import sys
@@ -136,6 +136,12 @@ def min(*a):  # noqa: A001
 
 def cast(x, dtype):
     return np.dtype(dtype).type(x)
+
+
+def random(dtype=None):
+    """ti.random() is 0.5 here: random perturbations of the form (random() - 0.5) * c vanish, so
+    a fixture pins everything but them."""
+    return np.float32(0.5)
 
 
 def atomic_add(ref, v):
