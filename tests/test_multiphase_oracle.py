@@ -193,3 +193,46 @@ def test_step_phase_indicator():
     _, _, u7 = orc.step(still, flags, f, phase=np.full(flags.shape, 0.7, f32))
     fl = (flags & 0x7) == 0
     assert np.allclose(u7[2][fl], 0.5 * 0.7 * -1e-4, rtol=1e-9)
+
+
+# ---- against the reference's own kernels (tests/golden/multiphase_reference.npz, made by
+# tests/golden/make_multiphase_golden.py, which runs multiphase_3d.py's kernel source in float32) ----
+def test_phase_kernels_match_reference_kernels():
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "multiphase_reference.npz"))
+    nx, ny, nz = z["phi"].shape
+    cfg = LatticeConfig(nx=nx, ny=ny, nz=nz)
+
+    def zyx(a):
+        return np.ascontiguousarray(a.transpose(2, 1, 0) if a.ndim == 3 else a.transpose(3, 2, 1, 0))
+    inner = np.zeros((nz, ny, nx), bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    phi = zyx(z["phi"])
+    sigma, width = float(z["sigma"]), float(z["width"])
+    mu = np.zeros_like(phi)
+    orc.phase_chemical_potential(cfg, phi, 3.0 * sigma * width / 8.0, mu)
+    assert np.allclose(mu[inner], zyx(z["mu"])[inner], rtol=0, atol=2e-6)
+    normal = np.zeros((3, nz, ny, nx), f32)
+    gmag = np.zeros_like(phi)
+    orc.phase_normals(cfg, phi, normal, gmag)
+    ref_n = zyx(z["normal"])
+    assert np.allclose(normal[:, inner], ref_n[:, inner], rtol=0, atol=1e-6)
+    assert np.allclose(gmag[inner], np.sqrt((zyx(z["grad_phi"]).astype(np.float64) ** 2).sum(0))[inner], atol=1e-6)
+    flags = zyx(z["solid"]).astype(np.uint32) * np.uint32(CELL_SOLID)
+    body = zyx(z["base"])
+    curv = np.zeros_like(phi)
+    sf = np.zeros_like(normal)
+    orc.phase_surface_tension(cfg, flags, phi, normal, gmag, zyx(z["rho"]), sigma, body, curv, sf)
+    assert np.allclose(curv[inner], zyx(z["curvature"])[inner], rtol=0, atol=2e-6)
+    assert np.allclose(sf, zyx(z["surface_force"]), rtol=0, atol=1e-8)
+    assert np.allclose(body, zyx(z["body_force"]), rtol=1e-6, atol=1e-9)
+    assert np.abs(zyx(z["surface_force"])).max() > 1e-5
+    # Cahn-Hilliard step with the phase separation, then the density and phase indicator
+    phi_new = np.zeros_like(phi)
+    rho = np.zeros_like(phi)
+    phase = np.zeros_like(phi)
+    orc.phase_update(cfg, np.zeros_like(flags), phi, phi_new, zyx(z["u"]), mu, float(z["mobility"]), 1.0,
+                     float(z["rho_air"]), float(z["rho_water"]), rho, phase)
+    assert np.allclose(phi_new, zyx(z["phi_new"]), rtol=0, atol=2e-6)
+    assert np.allclose(rho, zyx(z["rho_out"]), rtol=0, atol=2e-6)
+    assert np.allclose(phase, zyx(z["phase_out"]), rtol=0, atol=2e-6)
