@@ -89,6 +89,17 @@ def test_trilinear_linear_field_exact(orc):
     assert np.abs(out - pos).max() < 2e-6
 
 
+def test_trilinear_matches_reference_gather(orc):
+    """The reference's own interpolate_fluid_velocity_from_field run on a seeded field at 300
+    seeded positions, some outside the grid (tests/golden/trilinear_reference.npz, made by
+    tests/golden/make_trilinear_golden.py): same clamping, weights and sum order."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "trilinear_reference.npz"))
+    u = np.ascontiguousarray(z["u"].transpose(3, 2, 1, 0))  # (NX,NY,NZ,3) -> (3,NZ,NY,NX)
+    out = orc.trilinear(u, z["pos"])
+    assert np.array_equal(out, z["out"])  # bit for bit
+
+
 # ---- tests/test_under_relaxation.py ----------------------------------------------------------
 def test_under_relaxation_formula(orc):  # test_under_relaxation.py:108-134
     rng = np.random.default_rng(3)
