@@ -58,6 +58,8 @@ def load():
                          "orc_phase_update", "orc_phase_properties", "orc_pour_phase"):
                 getattr(lib, name).restype = None
             lib.orc_pour_advance.argtypes = [_v, _v]
+            lib.orc_set_legacy_feq_order.restype = None
+            lib.orc_set_legacy_feq_order.argtypes = [_i]
             _lib = lib
         return _lib
 
@@ -260,6 +262,21 @@ def porous_force(cfg, flags, rho, u):
     lib.orc_porous_force_f32(pp, _p(flags), _p(np.ascontiguousarray(rho, np.float32)),
                              _p(np.ascontiguousarray(u, np.float32)), _p(F))
     return F
+
+
+class legacy_feq_order:
+    """Context manager: inside it the oracle's collision builds f_eq for directions 7-18 with the
+    velocity table of the reference's lbm_algorithms.py (as its legacy collision does) while it
+    streams with config/core.py's.  Test-only: it reproduces a reference defect so that the rest of
+    the step can be pinned against the reference's own kernels."""
+
+    def __enter__(self):
+        load().orc_set_legacy_feq_order(1)
+        return self
+
+    def __exit__(self, *exc):
+        load().orc_set_legacy_feq_order(0)
+        return False
 
 
 def equilibrium(rho, u, dtype=np.float64):

@@ -59,6 +59,16 @@ T wq(int q) {
   return (T)WD[q];
 }
 
+// Test-only switch reproducing the reference legacy collision's mixed D3Q19 orderings: its f_eq
+// (equilibrium_d3q19_unified, lbm_algorithms.py:155-218) indexes the velocity table of
+// lbm_algorithms.py:158-164, whose entries 8/10 (y), 12/14 and 16/18 (z) are mirrored against the
+// config/core.py:36-38 table it streams with (legacy/lbm_solver.py:576 vs :617-619).  Off by
+// default: the build spec uses one ordering.  It exists so that the rest of the step can be pinned
+// against the reference's own kernels on states with flow in every direction.
+int g_legacy_feq_order = 0;
+const int ALG_CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 0, 0, 1, -1, 1, -1};
+const int ALG_CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+
 // Storage rounding of the shifted forms (f - w*rho0): FP16 is scaled by 2^12 so small
 // deviations stay normal numbers; BF16 needs no scale.
 const float F16_SCALE = 4096.0f;
@@ -318,6 +328,13 @@ void collide(const pog_params* p, const Geo& g, uint32_t flag, int i, int j, int
       Fz = Gz + Kvz - Kp * uz;
     }
     equilibrium<T>(rho, ux, uy, uz, feq);
+    if (g_legacy_feq_order) {
+      const T usq15 = (T)1.5 * (ux * ux + uy * uy + uz * uz);
+      for (int q = 7; q < 19; ++q) {
+        T eu = (T)CX[q] * ux + (T)ALG_CY[q] * uy + (T)ALG_CZ[q] * uz;
+        feq[q] = wq<T>(q) * rho * ((T)1 + (T)3 * eu + (T)4.5 * eu * eu - usq15);
+      }
+    }
     T tau0 = p->phase ? (ph > (T)0.5 ? (T)p->tau : (T)p->tau_air) : (T)p->tau;
     const bool les_on = !porous && !(p->phase && ph < (T)0.9 && ph > (T)-0.9);
     T nu = 0;
@@ -561,6 +578,7 @@ int orc_step_f64(const pog_params* p, const uint32_t* flags, const double* f, do
 }
 
 // ---- function-level helpers for the known-answer tests ------------------------------------
+void orc_set_legacy_feq_order(int on) { g_legacy_feq_order = on ? 1 : 0; }
 void orc_equilibrium_f64(double rho, double ux, double uy, double uz, double* feq) {
   equilibrium<double>(rho, ux, uy, uz, feq);
 }

@@ -7,7 +7,7 @@ Semantics: a `ti.kernel` or `ti.func` runs as the plain Python function it decor
 `ti.ndrange` is a nested range.  Fields are NumPy arrays of their dtype (f32 -> float32,
 i32 -> int32), so scalar arithmetic on field values stays in float32 as it does in Taichi (NumPy's
 promotion keeps float32 against Python scalars).  Vectors are float32 NumPy arrays with .x/.y/.z,
-.norm() and .dot().  `ti.random()` returns 0.5.  Parallel-for atomics, struct-for over fields,
+.norm() and .dot(); `ti.cast` of a vector is a vector of the new type.  `ti.random()` returns 0.5.  Parallel-for atomics, struct-for over fields,
 SNodes and autodiff are not provided: a generator that reaches them fails loudly.
 """
 import itertools
@@ -135,7 +135,14 @@ def min(*a):  # noqa: A001
 
 
 def cast(x, dtype):
+    if isinstance(x, np.ndarray) and x.ndim:
+        return Vector(x, dtype)
     return np.dtype(dtype).type(x)
+
+
+def loop_config(**_):
+    """Launch hints (block_dim ...) have no meaning for serial execution."""
+    return None
 
 
 def random(dtype=None):
@@ -156,7 +163,12 @@ cpu = gpu = cuda = vulkan = metal = "stand-in"
 
 
 def install():
-    """Register this module as `taichi` for the reference's `import taichi as ti`."""
+    """Register this module as `taichi` for the reference's `import taichi as ti`.
+
+    Float32 field arithmetic stays float32 only under NumPy 2's promotion rules (NEP 50: a Python
+    float does not widen an np.float32); under NumPy 1 it would silently become float64."""
+    if int(np.__version__.split(".")[0]) < 2:
+        raise RuntimeError("the Taichi stand-in needs NumPy >= 2 (float32 scalar promotion, NEP 50)")
     sys.modules["taichi"] = sys.modules[__name__]
     return sys.modules[__name__]
 
