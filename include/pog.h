@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define POG_VERSION 1
+#define POG_VERSION 2
 
 /* ---- error codes ---------------------------------------------------------------------- */
 #define POG_OK 0
@@ -138,6 +138,15 @@ typedef struct pog_params {
    * pog_particles_clear_deposit clears them).  With a mask the step reads pdrag only at set bits
    * and takes zero elsewhere; the caller keeps pdrag zero wherever the bit is clear. */
   const uint32_t* deposit_mask;
+  /* Optional DEVICE list of the cells pog_wall_list returns (fluid cells with a solid neighbour),
+   * n_wall_cells entries, or NULL.  Non-null selects the row-tiled step kernel in pog_step: whole
+   * grid rows staged through shared memory by bulk TMA copies, bounce-back through per-link
+   * mailbox slots copied by a pass over these cells around each odd step.  It needs nx * element
+   * size to be a multiple of 16 bytes, nx <= 320 and a 16-byte aligned distribution buffer, and
+   * serves FP32/FP16S/BF16S storage; otherwise pog_step takes the register-staged kernel.  Both
+   * compute the same update and leave the same state between steps. */
+  const int32_t* wall_cells;
+  int32_t n_wall_cells;
 } pog_params;
 
 /* Pour-nozzle block, floats (PrecisePouringSystem, src/physics/precise_pouring.py:12-193):
@@ -202,7 +211,23 @@ typedef struct pog_particle_params {
   /* Optional DEVICE bit mask [ceil(ncell/32)] or NULL: the coupling pass sets bit c for every
    * cell it deposits into (see pog_params.deposit_mask). */
   uint32_t* deposit_mask;
+  /* How the particles act on the fluid (enum pog_reaction). */
+  int32_t reaction;
 } pog_particle_params;
+
+/* Particle-to-fluid exchange of pog_particles_couple.  The deposit pdrag = (Kp, Kv) enters the
+ * step as the force Kv - Kp u with u implicit, so an explicit force is a deposit with Kp = 0. */
+enum pog_reaction {
+  POG_REACTION_IMPLICIT = 0,     /* Kp = w beta, Kv = w beta v_new: the drag beta (v_new - u)
+                                    taken with the fluid's updated u (stable at any loading)     */
+  POG_REACTION_EXPLICIT = 1,     /* Kp = 0, Kv = -w F: the reaction of the relaxed drag F that
+                                    moves the particle, spread with the trilinear weights
+                                    (distribute_force_to_grid, coffee_particles.py:1048-1086,
+                                    added as a body force, legacy/lbm_solver.py:1478-1483)       */
+  POG_REACTION_EXPLICIT_NEW = 2  /* Kp = 0, Kv = -w F_new: the reaction of the unrelaxed drag, as
+                                    compute_two_way_coupling_forces spreads it
+                                    (coffee_particles.py:1141-1149)                               */
+};
 
 /* ---- library ------------------------------------------------------------------------------- */
 int pog_version(void);
@@ -343,12 +368,21 @@ int pog_init_equilibrium(const pog_params* p, void* f, const uint32_t* flags, fl
  *   rho_out, u_out  macroscopic output (rho and Guo-corrected u of the incoming state) of
  *              the LAST step, or NULL
  *   reductions POG_RED_COUNT doubles accumulated over all nsteps, or NULL
- * Kernel: the register-staged step; the environment variable POG_AA_KERNEL=tma selects the
- * TMA-staged step (bulk copies of the 19 planes through a shared-memory ring, warp-specialised)
- * when f is 16-byte aligned.  Both compute the same update. */
+ * Kernel: the row-tiled TMA-staged step when p->wall_cells is set and applies (see pog_params),
+ * else the register-staged step.  Both compute the same update. */
 int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, int nsteps,
              const float* force, const float* pdrag, const float* porosity, float* u_prev, float* u_next,
              float* rho_out, float* u_out, double* reductions, void* stream);
+
+/* The cells the row-tiled step's bounce-back mailbox pass serves: fluid cells with at least one
+ * solid neighbour on the planes 1 .. nz-2 with 1 <= i <= nx-2, derived from the flag words (the
+ * link bits replace the solid-neighbour tests of legacy/lbm_solver.py:621-628).  `count` is a
+ * DEVICE int32 that receives the number of such cells; up to `capacity` of them are written to
+ * `cells` (DEVICE, nullable: count only).  The order of the list is unspecified (the mailbox
+ * copies are independent of one another).  Call once with cells NULL, read the count, allocate,
+ * call again. */
+int pog_wall_list(const pog_params* p, const uint32_t* flags, int32_t* cells, int32_t capacity,
+                  int32_t* count, void* stream);
 
 /* Same step on the natural (two-buffer) layout: reads f_in at time t, writes f_out at t+1
  * with push streaming exactly as legacy/lbm_solver.py:609-628.  Used for checkpointed
@@ -386,12 +420,15 @@ int pog_particles_bin(const pog_params* p, const float* pos, const int32_t* acti
 /* Same binning and stable cell sort as pog_particles_bin, but it allocates nothing and takes
  * no scratch argument: for callers that may not allocate device memory once running (a host
  * application that gives the library a fixed device-memory budget, or a loop that must not block
- * on an allocator).  Its scratch is a fixed device array inside libpog.so, reserved on every GPU
- * that loads the library until the process exits.  Limit: np <= POG_NOALLOC_MAX_PARTICLES
- * (larger np returns POG_E_RANGE).  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU race and must be
- * ordered by the caller.  No counterpart in the reference (it has no sort and no scratch). */
+ * on an allocator).  Its scratch is a fixed 20 MiB device array inside libpog.so.  CUDA loads the
+ * library's device code lazily, so the array is reserved on a GPU by the first call on that GPU,
+ * which also looks up its address (cudaGetSymbolAddress) with that device current, and stays
+ * reserved until the process exits: make one call with np = 0 on each device at set-up time,
+ * before the memory budget is fixed and before any stream capture.  Limit: np <=
+ * POG_NOALLOC_MAX_PARTICLES (larger np returns POG_E_RANGE).  The current device must be the
+ * stream's device; the cached address does not survive cudaDeviceReset.  All calls share the
+ * array: calls that overlap on the GPU race and must be ordered by the caller.  No counterpart in
+ * the reference (it has no sort and no scratch). */
 #define POG_NOALLOC_MAX_PARTICLES (1 << 20)
 int pog_particles_bin_noalloc(const pog_params* p, const float* pos, const int32_t* active, int np,
                               int32_t* keys, int32_t* perm, void* stream);
@@ -430,14 +467,25 @@ int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* 
 /* Reverse of one pog_step_push step (natural layout, storage F32 or F64).
  *   f_t       forward state at time t (natural), the input of the step being reversed
  *   lam_next  adjoint of the state at t+1;  lam_t  receives the adjoint at t
+ *   pdrag     [4][ncell] the particle drag deposit (Kp, Kv) the forward step read, or NULL: a
+ *             fixed input, its force Kv - Kp u differentiated through u (the coupled step of
+ *             legacy/lbm_solver.py:1485-1509 with the particles' deposit recorded per step)
  *   The loss is J = sum_t flux_t with flux_t = POG_RED_OUTFLOW of step t, so each outlet
  *   cell adds dJ/df_i = -c_iz.  Parameter gradients are accumulated in FP64:
  *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
  *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL,
  *   pour_control, filter_blockage and phase NULL (POG_E_ARG otherwise). */
 int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next, void* lam_t,
-                     const uint32_t* flags, const float* porosity, double* grad_porosity,
-                     double* grad_inlet, void* stream);
+                     const uint32_t* flags, const float* porosity, const float* pdrag,
+                     double* grad_porosity, double* grad_inlet, void* stream);
+
+/* The outflow flux of a natural-layout state f_nat (F32 or F64 storage), flux = -sum over outlet
+ * cells of sum_q c_qz f_q -- the POG_RED_OUTFLOW contribution of the step that starts from f_nat --
+ * added to *acc (DEVICE int64) in fixed point, units of 2^-48.  Integer sums do not depend on the
+ * order of accumulation, so a loss J = sum_t flux_t built from it is the same bits on every run
+ * (finite differences of J then carry no reduction-order noise). */
+int pog_outflow_fixed(const pog_params* p, const void* f_nat, const uint32_t* flags, long long* acc,
+                      void* stream);
 
 #ifdef __cplusplus
 }

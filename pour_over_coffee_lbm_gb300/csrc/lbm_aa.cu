@@ -252,21 +252,10 @@ static int dispatch_storage(const KParams& kp, int parity, bool reduce, bool mac
   return set_error(POG_E_ARG, "storage %d unknown", kp.storage);
 }
 
-int launch_aa_tma(const KParams& kp, int parity, bool reduce, void* f, const uint32_t* flags,
-                  const float* force, const float* pdrag, const float* eps, const float* u_prev, float* u_next,
-                  float* rho_out, float* u_out, double* red, cudaStream_t s);
-
-// Which step kernel pog_step uses: the register-staged one (default: measured faster on GB300)
-// or the TMA-staged one (POG_AA_KERNEL=tma, needs a 16-byte aligned distribution buffer; kept
-// for A/B timing).  Both compute the same update.
-static bool use_tma(const void* f) {
-  static int mode = -1;
-  if (mode < 0) {
-    const char* e = getenv("POG_AA_KERNEL");
-    mode = (e && e[0] == 't') ? 1 : 0;
-  }
-  return mode == 1 && ((uintptr_t)f & 15u) == 0;
-}
+int launch_rows_step(const KParams& kp, int parity, bool reduce, void* f, const uint32_t* flags,
+                     const int32_t* cells, int32_t ncells, const float* force, const float* pdrag, const float* eps,
+                     const float* u_prev, float* u_next, float* rho_out, float* u_out, double* red,
+                     cudaStream_t s);
 
 static int grid_for(uint32_t n, int block) {
   long long want = ((long long)n + block - 1) / block;
@@ -329,11 +318,13 @@ int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, i
   for (int i = 0; i < nsteps; ++i) {
     const bool last = i == nsteps - 1;
     const int parity = (int)((t + i) & 1);
-    if (use_tma(f))
-      rc = launch_aa_tma(kp, parity, reductions != nullptr, f, flags, force, pdrag, porosity,
-                         stencil ? up : nullptr, stencil ? un : nullptr, last ? rho_out : nullptr,
-                         last ? u_out : nullptr, reductions, s);
-    else
+    // the row-tiled kernel when the caller supplied the bounce-back cell list (and it applies)
+    rc = 1;
+    if (p->wall_cells)
+      rc = launch_rows_step(kp, parity, reductions != nullptr, f, flags, p->wall_cells, p->n_wall_cells, force,
+                            pdrag, porosity, stencil ? up : nullptr, stencil ? un : nullptr,
+                            last ? rho_out : nullptr, last ? u_out : nullptr, reductions, s);
+    if (rc == 1)
       rc = dispatch_storage(kp, parity, reductions != nullptr, false, f, flags, force, pdrag, porosity,
                             stencil ? up : nullptr, stencil ? un : nullptr,
                             last ? rho_out : nullptr, last ? u_out : nullptr,

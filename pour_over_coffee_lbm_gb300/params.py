@@ -14,6 +14,7 @@ STORE_F32, STORE_F16S, STORE_BF16S, STORE_F64 = 0, 1, 2, 3
 STORAGE_NAMES = {"f32": STORE_F32, "f16s": STORE_F16S, "bf16s": STORE_BF16S, "f64": STORE_F64}
 LES_OFF, LES_STENCIL, LES_LOCAL = 0, 1, 2
 DRAG_SEMI_IMPLICIT, DRAG_EXPLICIT_CAP = 0, 1
+REACTION_IMPLICIT, REACTION_EXPLICIT, REACTION_EXPLICIT_NEW = 0, 1, 2
 FORCING_GUO, FORCING_REFERENCE = 0, 1
 INLET_NCOEF = 16
 
@@ -45,6 +46,7 @@ class PogParams(ctypes.Structure):
         ("filter_blockage", ctypes.c_void_p),
         ("phase", ctypes.c_void_p), ("tau_air", ctypes.c_float),
         ("deposit_mask", ctypes.c_void_p),
+        ("wall_cells", ctypes.c_void_p), ("n_wall_cells", ctypes.c_int32),
     ]
 
 
@@ -55,6 +57,7 @@ class PogParticleParams(ctypes.Structure):
         ("wall_margin", ctypes.c_float), ("wall_pullback", ctypes.c_float),
         ("wall_damping", ctypes.c_float), ("z_floor", ctypes.c_float),
         ("deposit_cells", ctypes.c_void_p), ("deposit_mask", ctypes.c_void_p),
+        ("reaction", ctypes.c_int32),
     ]
 
 
@@ -149,6 +152,7 @@ class ParticleConfig:
     z_floor: float = 3.0
     seed: int = 1234
     sort_interval: int = 20
+    reaction: int = REACTION_IMPLICIT
 
     def to_c(self) -> PogParticleParams:
         pp = PogParticleParams()
@@ -161,6 +165,7 @@ class ParticleConfig:
         pp.wall_pullback = self.wall_pullback
         pp.wall_damping = self.wall_damping
         pp.z_floor = self.z_floor
+        pp.reaction = int(self.reaction)
         return pp
 
 

@@ -125,7 +125,8 @@ class GB300LBMSolver:
     mask, stepped by libpog.so on one GB300 (sm_103a)."""
 
     def __init__(self, config: Optional[LatticeConfig] = None, device: str = "cuda",
-                 porosity: Optional[np.ndarray] = None, preferred_backend: Optional[str] = None):
+                 porosity: Optional[np.ndarray] = None, preferred_backend: Optional[str] = None,
+                 step_kernel: str = "registers"):
         if not torch.cuda.is_available():
             raise RuntimeError("GB300LBMSolver needs a CUDA device (no CPU path exists)")
         self.lib = _lib.load()
@@ -142,6 +143,14 @@ class GB300LBMSolver:
         # one 32-bit word per cell: flag bits + bit (8+q) when neighbour q is solid
         self._flags = torch.empty(shape, dtype=torch.int32, device=dev)
         self._build_flags()
+        # "registers" (default, measured faster on GB300): the register-staged step; "rows": the
+        # row-tiled TMA-staged step (with its bounce-back cell list) where it applies.  Same update
+        # either way.
+        if step_kernel not in ("rows", "registers"):
+            raise ValueError("step_kernel must be 'rows' or 'registers'")
+        self.step_kernel = step_kernel
+        self._walls = None
+        self._build_wall_list()
         self._f = torch.empty((19,) + shape, dtype=_STORAGE_DTYPE[c.storage], device=dev)
         self._rho = torch.ones(shape, dtype=torch.float32, device=dev)
         self._u = torch.zeros((3,) + shape, dtype=torch.float32, device=dev)
@@ -188,6 +197,23 @@ class GB300LBMSolver:
 
     def _build_flags(self):
         _lib.check(self.lib.pog_build_flags(self._p, _lib.ptr(self._flags), self._s()))
+
+    def _build_wall_list(self):
+        """The cells of the row-tiled step's bounce-back mailbox pass (pog_wall_list), kept on
+        the device and referenced from the parameter block."""
+        self._walls = None
+        self._p.wall_cells = None
+        self._p.n_wall_cells = 0
+        if self.step_kernel != "rows":
+            return
+        count = torch.zeros(1, dtype=torch.int32, device=self.device)
+        _lib.check(self.lib.pog_wall_list(self._p, _lib.ptr(self._flags), None, 0, _lib.ptr(count), self._s()))
+        n = int(count.item())
+        self._walls = torch.empty(max(n, 1), dtype=torch.int32, device=self.device)
+        _lib.check(self.lib.pog_wall_list(self._p, _lib.ptr(self._flags), _lib.ptr(self._walls), n,
+                                          _lib.ptr(count), self._s()))
+        self._p.wall_cells = self._walls.data_ptr()
+        self._p.n_wall_cells = n
 
     def _refresh_macro(self):
         """Recompute the moments the next read needs: rho and u when the state changed since they
@@ -342,6 +368,7 @@ class GB300LBMSolver:
             links |= nb_solid.astype(np.uint32) << np.uint32(8 + q)
         fl = np.where(~solid & (links != 0), fl | CELL_NEAR_SOLID | links, fl).astype(np.uint32)
         self._flags.copy_(torch.from_numpy(fl.astype(np.int32)))
+        self._build_wall_list()
         self.initialize_fields(self.cfg.rho0)
 
     def set_porosity(self, eps) -> None:
@@ -588,7 +615,11 @@ class GB300LBMSolver:
         if mode == LES_STENCIL and self._ul is None:
             self._ul = [self._u.clone(), self._u.clone()]
         self.cfg = self.cfg.replace(les_mode=mode, cs_smag=float(smagorinsky_constant))
-        self._p = self.cfg.to_c()
+        p = self.cfg.to_c()
+        for name in ("inlet_control", "pour_control", "filter_blockage", "phase", "deposit_mask",
+                     "wall_cells", "n_wall_cells", "tau_air"):
+            setattr(p, name, getattr(self._p, name))
+        self._p = p
         self.use_les = True
 
     def export_vtk(self, filename: str) -> None:

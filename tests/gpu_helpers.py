@@ -39,14 +39,30 @@ def gpu_flags(cfg):
     return fl
 
 
+def wall_list(p, flags):
+    """The row-tiled step's bounce-back cell list (pog_wall_list: count, allocate, fill)."""
+    count = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _lib.check(lib().pog_wall_list(ctypes.byref(p), P(flags), None, 0, P(count), S()))
+    n = int(count.item())
+    cells = torch.empty(n, dtype=torch.int32, device="cuda")
+    _lib.check(lib().pog_wall_list(ctypes.byref(p), P(flags), P(cells) if n else None, n, P(count), S()))
+    assert int(count.item()) == n
+    return cells
+
+
 class AARun:
     """AA-pattern state driven through pog_step."""
 
-    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None):
+    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None, rows=False):
         self.cfg = cfg
         self.p = cfg.to_c()
         shape = (cfg.nz, cfg.ny, cfg.nx)
         self.flags = gpu_flags(cfg) if flags is None else torch.as_tensor(np.asarray(flags).astype(np.int32)).cuda()
+        self.walls = None
+        if rows:
+            self.walls = wall_list(self.p, self.flags)
+            self.p.wall_cells = P(self.walls)
+            self.p.n_wall_cells = int(self.walls.numel()) if self.walls.numel() > 0 else 0
         self.f = torch.empty((19,) + shape, dtype=DT[cfg.storage], device="cuda")
         self.rho = torch.zeros(shape, dtype=torch.float32, device="cuda")
         self.u = torch.zeros((3,) + shape, dtype=torch.float32, device="cuda")
@@ -79,8 +95,8 @@ class AARun:
         return nat.cpu().numpy()
 
 
-def run_aa(cfg, steps, eps=None, force=None, reduce=True, pdrag=None):
-    r = AARun(cfg, eps=eps, force=force, pdrag=pdrag)
+def run_aa(cfg, steps, eps=None, force=None, reduce=True, pdrag=None, rows=False):
+    r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows)
     if steps > 1:
         r.step(steps - 1, reduce=reduce, macro=False)
     r.step(1, reduce=reduce, macro=True)

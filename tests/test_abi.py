@@ -39,7 +39,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_version_and_errors():
     lib = _lib.load()
-    assert lib.pog_version() == 1
+    assert lib.pog_version() == 2
     p = LatticeConfig(nx=2).to_c()
     rc = lib.pog_validate_params(ctypes.byref(p))
     assert rc == -1
