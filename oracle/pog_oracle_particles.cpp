@@ -178,9 +178,10 @@ int orc_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
     }
     float gvec[3] = {p->gx, p->gy, p->gz};
     float beta = mp / (taup + dt);  // drag coefficient: F_new = beta (u_f - v)
-    float F[3];
+    float F[3], Fn[3];
     for (int a = 0; a < 3; ++a) {
       float fnew = mp * ur[a] / (taup + dt);
+      Fn[a] = fnew;
       F[a] = alpha * fnew + (1.0f - alpha) * drag_old[a * np + q];
       drag_old[a * np + q] = F[a];
     }
@@ -248,8 +249,15 @@ int orc_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
       vel[a * np + q] = nv[a];
     }
     // deposit Kp += w beta, Kv += w beta v_new on the 8 nodes of the gather position; the lattice
-    // step takes the particle force on the fluid, Kv - Kp u, implicitly
+    // step takes the particle force on the fluid, Kv - Kp u, implicitly.  The explicit reactions
+    // deposit Kp = 0, Kv = -w F (relaxed drag) or -w F_new (unrelaxed; distribute_force_to_grid,
+    // coffee_particles.py:1048-1086 called at :1145-1149), which the step adds as a body force.
     float dep[4] = {beta, beta * nv[0], beta * nv[1], beta * nv[2]};
+    if (pp->reaction != POG_REACTION_IMPLICIT) {
+      const float* R = pp->reaction == POG_REACTION_EXPLICIT ? F : Fn;
+      dep[0] = 0.0f;
+      for (int a = 0; a < 3; ++a) dep[1 + a] = -R[a];
+    }
     for (int a = 0; a < 4; ++a)
       for (int c = 0; c < 8; ++c) {
         float contrib = w[c] * dep[a];

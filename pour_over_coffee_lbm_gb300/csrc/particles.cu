@@ -186,6 +186,7 @@ struct PKParams {
   float rho0, mu, rho_p, alpha, dt, gx, gy, gz;
   float zlo, zhi, margin, pullback, damping;
   int drag_model, deterministic;
+  int reaction;       // enum pog_reaction
   const float* pour;  // device pour-nozzle block or null
   int32_t* dep_cells;  // device [np]: base cell of each particle's deposit (-1: none) or null
   uint32_t* dmask;     // device bit mask of the deposited cells or null
@@ -292,7 +293,8 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
     int i = 0, j = 0, k = 0;
     float w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     float F[3] = {0, 0, 0};
-    float dep[4] = {0, 0, 0, 0};  // deposit: beta, beta * v_new
+    float Fn[3] = {0, 0, 0};      // unrelaxed drag F_new
+    float dep[4] = {0, 0, 0, 0};  // deposit (Kp, Kv): beta, beta * v_new; or 0, -F
     bool dep_ok = false;
     if (ok) {
       x = pos[q];
@@ -353,6 +355,7 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         float fnew = mp * ur[a] / (taup + P.dt);
+        Fn[a] = fnew;
         F[a] = P.alpha * fnew + (1.0f - P.alpha) * drag_old[a * np + q];
         drag_old[a * np + q] = F[a];
       }
@@ -398,9 +401,15 @@ __global__ void couple_kernel(PKParams P, float* __restrict__ pos, float* __rest
           pos[a * np + q] = np3[a];
           vel[a * np + q] = nv[a];
         }
-        dep[0] = beta;
+        if (P.reaction == POG_REACTION_IMPLICIT) {
+          dep[0] = beta;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) dep[1 + a] = beta * nv[a];
+          for (int a = 0; a < 3; ++a) dep[1 + a] = beta * nv[a];
+        } else {
+          // Newton's third law as an explicit body force (Kp stays 0)
+#pragma unroll
+          for (int a = 0; a < 3; ++a) dep[1 + a] = -(P.reaction == POG_REACTION_EXPLICIT ? F[a] : Fn[a]);
+        }
         dep_ok = true;
       }
     }
@@ -565,6 +574,8 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
     return set_error(POG_E_ARG, "a particle array or u is NULL");
   if (pp->deterministic ? !pdrag_fix : !pdrag)
     return set_error(POG_E_ARG, "drag accumulator for the selected mode is NULL");
+  if (pp->reaction < POG_REACTION_IMPLICIT || pp->reaction > POG_REACTION_EXPLICIT_NEW)
+    return set_error(POG_E_ARG, "reaction %d unknown", pp->reaction);
   PKParams P;
   P.nx = p->nx;
   P.ny = p->ny;
@@ -590,6 +601,7 @@ int pog_particles_couple(const pog_params* p, const pog_particle_params* pp, flo
   P.damping = pp->wall_damping;
   P.drag_model = pp->drag_model;
   P.deterministic = pp->deterministic;
+  P.reaction = pp->reaction;
   P.pour = p->pour_control;
   P.dep_cells = pp->deposit_cells;
   P.dmask = pp->deposit_mask;

@@ -136,8 +136,10 @@ class CoffeeParticleSystem:
                pdrag: Optional[torch.Tensor] = None, deposit_mask: Optional[torch.Tensor] = None):
         """One coupling pass against solver's current velocity field: drag, under-relaxation,
         integration, and the drag deposit (Kp, Kv) added into `pdrag` ([4, NZ, NY, NX], not
-        cleared here) for the implicit fluid-side force of the next lattice step.  deposit_mask
-        (int32 [ceil(ncell/32)]): the bits of the deposited cells are set."""
+        cleared here) for the fluid-side force Kv - Kp u of the next lattice step: the implicit
+        drag by default, or with config.reaction = REACTION_EXPLICIT(_NEW) the reaction -F spread
+        as an explicit body force (Kp = 0), as the reference's distribute_force_to_grid does.
+        deposit_mask (int32 [ceil(ncell/32)]): the bits of the deposited cells are set."""
         n = self.count
         if n == 0:
             return
@@ -147,7 +149,7 @@ class CoffeeParticleSystem:
         # the parameter block is rebuilt only when one of its inputs changes
         mptr = None if deposit_mask is None else deposit_mask.data_ptr()
         key = (pc.density_ratio, pc.drag_model, pc.deterministic, pc.wall_margin, pc.wall_pullback,
-               pc.wall_damping, pc.z_floor, dt, relaxation_factor, mptr)
+               pc.wall_damping, pc.z_floor, pc.reaction, dt, relaxation_factor, mptr)
         if self._pp_key != key:
             pp = pc.to_c()
             pp.dt = float(dt)

@@ -132,7 +132,15 @@ def test_plain_64_fp32_200_steps(cuda, orc):
     _, _, rho64, u64 = orc.run(cfg.replace(storage=STORE_F64), 200, np.float64)
     fluid = (flags & CELL_SOLID) == 0
     e_gpu, e_orc = _fp32_bar(r.u.cpu().numpy(), u32, u64, r.rho.cpu().numpy(), rho32, fluid)
-    assert e_gpu < 1e-3
+    d = rel_l2(r.u.cpu().numpy()[:, fluid], u32[:, fluid])
+    print("64^3 FP32, 200 steps, u relative L2: GPU vs FP64 oracle %.3e; FP32 oracle vs FP64 oracle %.3e; "
+          "GPU vs FP32 oracle %.3e" % (e_gpu, e_orc, d))
+    # absolute numbers: the GPU stores the shifted deviations f - w rho0 and sits close to FP64
+    # (about 1e-6); the plain-FP32 oracle resolves u only to 1.8e-4 here, so the distance between
+    # the two is the oracle's own rounding
+    assert e_gpu < 2e-5
+    assert 1e-4 < e_orc < 3e-4
+    assert d < 3e-4
 
 
 def test_fp32_les_porous_eps_vs_oracle(cuda, orc):
