@@ -34,7 +34,7 @@ def load():
             for name in ("orc_build_flags", "orc_init_equilibrium_f32", "orc_step_f32",
                          "orc_step_f64", "orc_les_nu_f32", "orc_porous_force_f32",
                          "orc_particles_bin", "orc_particles_couple", "orc_trilinear_f32",
-                         "orc_adjoint_step_f64", "orc_d3q19_tables"):
+                         "orc_adjoint_step_f64", "orc_d3q19_tables", "orc_step_aa_f32", "orc_step_aa_f64"):
                 getattr(lib, name).restype = _i
             lib.orc_init_equilibrium_f64.restype = _i
             lib.orc_init_equilibrium_f64.argtypes = [_v, _v, _v, ctypes.c_double, ctypes.c_double,
@@ -231,6 +231,26 @@ def step(cfg, flags, f, force=None, eps=None, u_prev=None, reductions=None, pdra
     return fo, rho, u
 
 
+def step_aa(cfg, flags, f, t, force=None, eps=None, pdrag=None, reductions=None, macro=False):
+    """One AA-pattern step of f (AA layout, [19, NZ, NY, NX] float32 or float64, C-contiguous) in
+    place at time t.  Returns (rho, u) of the step when macro, else None."""
+    assert f.flags.c_contiguous and f.dtype in (np.float32, np.float64)
+    lib = load()
+    _keep, pp = _params(cfg)
+    dt = f.dtype
+    rho = np.zeros((cfg.nz, cfg.ny, cfg.nx), dt) if macro else None
+    u = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), dt) if macro else None
+    force = None if force is None else np.ascontiguousarray(force, np.float32)
+    eps = None if eps is None else np.ascontiguousarray(eps, np.float32)
+    pdrag = None if pdrag is None else np.ascontiguousarray(pdrag, np.float32)
+    fn = lib.orc_step_aa_f64 if dt == np.float64 else lib.orc_step_aa_f32
+    rc = fn(pp, _p(np.ascontiguousarray(flags, np.uint32)), _p(f), ctypes.c_longlong(t), _p(force), _p(pdrag),
+            _p(eps), _p(rho), _p(u), _p(reductions))
+    if rc != 0:
+        raise ValueError("the AA step restatement supports les_mode OFF or LOCAL")
+    return (rho, u) if macro else None
+
+
 def run(cfg, nsteps, dtype=np.float64, flags=None, force=None, eps=None, reductions=None):
     """nsteps from equilibrium.  Returns (flags, f, rho, u) of the last step (rho/u are the
     moments computed inside that step)."""
@@ -351,14 +371,18 @@ def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=N
     return pos, vel, drag_old, active, force_fix, u_at
 
 
-def adjoint_step(cfg, flags, f_t, lam_next, eps=None, grad_eps=None, grad_inlet=None):
+def adjoint_step(cfg, flags, f_t, lam_next, eps=None, grad_eps=None, grad_inlet=None, pdrag=None):
+    """Adjoint of one FP64 push step by forward-mode dual numbers; pdrag: the step's particle drag
+    deposit [4][n] (float32), held fixed."""
     lib = load()
     _, pp = _params(cfg)
     lam_t = np.zeros_like(lam_next)
     if eps is not None:
         eps = np.ascontiguousarray(eps, np.float32)
+    if pdrag is not None:
+        pdrag = np.ascontiguousarray(pdrag, np.float32)
     lib.orc_adjoint_step_f64(pp, _p(flags), _p(np.ascontiguousarray(f_t, np.float64)),
-                             _p(np.ascontiguousarray(lam_next, np.float64)), _p(lam_t), _p(eps),
+                             _p(np.ascontiguousarray(lam_next, np.float64)), _p(lam_t), _p(eps), _p(pdrag),
                              _p(grad_eps), _p(grad_inlet))
     return lam_t
 

@@ -475,6 +475,83 @@ int step_push(const pog_params* p, const uint32_t* flags, const T* f, T* fo, con
   return 0;
 }
 
+// One AA-pattern step in place (the CUDA step's stepping order, Bailey et al. 2009): at an even
+// time t slot (c, q) holds f_q(c), the step reads it and writes f*_q to (c, opp q); at an odd t
+// the step reads f_q from (c - e_q, opp q) -- or (c, q) when c - e_q is solid -- and writes f*_q
+// to (c + e_q, q) -- or (c, opp q) when c + e_q is solid.  Each cell reads and writes the same 19
+// slots, so the cells are independent.  Cells within one plane + row + 1 of either end of the
+// grid are never updated (the CUDA kernels' guard).  The collision is `collide`, as in step_push.
+template <typename T>
+int step_aa(const pog_params* p, const uint32_t* flags, T* f, long long t, const float* Fe, const float* Pd,
+            const float* eps, T* rho_out, T* u_out, double* red) {
+  Geo g = make_geo(p);
+  const long long n = g.n;
+  const long long guard = (long long)g.nx * g.ny + g.nx + 1;
+  const bool odd = (t & 1) != 0;
+  double acc[POG_RED_COUNT] = {0, 0, 0, 0, 0, 0};
+  const T rho0 = (T)p->rho0;
+#pragma omp parallel
+  {
+    double loc[POG_RED_COUNT] = {0, 0, 0, 0, 0, 0};
+#pragma omp for schedule(static)
+    for (int k = 0; k < g.nz; ++k)
+      for (int j = 0; j < g.ny; ++j)
+        for (int i = 0; i < g.nx; ++i) {
+          const long long c = g.idx(i, j, k);
+          const uint32_t fl = flags[c];
+          if ((fl & POG_CELL_SOLID) || c < guard || c > n - 1 - guard) continue;
+          T fin[19], fs[19], rho, u[3];
+          for (int q = 0; q < 19; ++q) {
+            if (!odd) {
+              fin[q] = f[q * n + c];
+            } else {
+              const long long src = g.idx(i - CX[q], j - CY[q], k - CZ[q]);
+              fin[q] = (q != 0 && (flags[src] & POG_CELL_SOLID)) ? f[q * n + c] : f[OPP[q] * n + src];
+            }
+          }
+          T fe[3];
+          const T* fep = nullptr;
+          if (Fe) {
+            fe[0] = (T)Fe[c];
+            fe[1] = (T)Fe[n + c];
+            fe[2] = (T)Fe[2 * n + c];
+            fep = fe;
+          }
+          T pd[4];
+          const T* pdp = nullptr;
+          if (Pd) {
+            for (int a = 0; a < 4; ++a) pd[a] = (T)Pd[a * n + c];
+            pdp = pd;
+          }
+          collide<T>(p, g, fl, i, j, k, fin, fep, pdp, eps != nullptr, eps ? (T)eps[c] : (T)0, (T)0, fs, rho, u,
+                     red ? loc : nullptr);
+          if (rho_out) rho_out[c] = rho;
+          if (u_out) {
+            u_out[c] = u[0];
+            u_out[n + c] = u[1];
+            u_out[2 * n + c] = u[2];
+          }
+          for (int q = 0; q < 19; ++q) {
+            const T v = store_round<T>(p->storage, fs[q], q, rho0);
+            if (!odd) {
+              f[OPP[q] * n + c] = v;
+            } else {
+              const long long dst = g.idx(i + CX[q], j + CY[q], k + CZ[q]);
+              if (q != 0 && (flags[dst] & POG_CELL_SOLID))
+                f[OPP[q] * n + c] = v;
+              else
+                f[q * n + dst] = v;
+            }
+          }
+        }
+#pragma omp critical
+    for (int r = 0; r < POG_RED_COUNT; ++r) acc[r] += loc[r];
+  }
+  if (red)
+    for (int r = 0; r < POG_RED_COUNT; ++r) red[r] += acc[r];
+  return 0;
+}
+
 template <typename T>
 void init_eq(const pog_params* p, const uint32_t* flags, T* f, T rho0, T ux, T uy, T uz) {
   Geo g = make_geo(p);
@@ -575,6 +652,19 @@ int orc_step_f64(const pog_params* p, const uint32_t* flags, const double* f, do
                  const float* Fe, const float* Pd, const float* eps, const double* u_prev,
                  double* rho_out, double* u_out, double* red) {
   return step_push<double>(p, flags, f, fo, Fe, Pd, eps, u_prev, rho_out, u_out, red);
+}
+
+// In-place AA-pattern step at time t (les_mode OFF or LOCAL: the stencil mode's u history is the
+// push step's business).
+int orc_step_aa_f32(const pog_params* p, const uint32_t* flags, float* f, long long t, const float* Fe,
+                    const float* Pd, const float* eps, float* rho_out, float* u_out, double* red) {
+  if (p->les_mode == POG_LES_STENCIL) return -1;
+  return step_aa<float>(p, flags, f, t, Fe, Pd, eps, rho_out, u_out, red);
+}
+int orc_step_aa_f64(const pog_params* p, const uint32_t* flags, double* f, long long t, const float* Fe,
+                    const float* Pd, const float* eps, double* rho_out, double* u_out, double* red) {
+  if (p->les_mode == POG_LES_STENCIL) return -1;
+  return step_aa<double>(p, flags, f, t, Fe, Pd, eps, rho_out, u_out, red);
 }
 
 // ---- function-level helpers for the known-answer tests ------------------------------------
@@ -980,9 +1070,11 @@ inline Dual sqrt(const Dual& a) {
 }
 }  // namespace
 
+// Pd (nullable): the step's particle drag deposit [4][n] (Kp, Kv), a fixed input (constants in
+// the dual numbers), as the CUDA adjoint takes it.
 extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint32_t* flags, const double* ft,
                                     const double* lam_next, double* lam_t, const float* eps,
-                                    double* grad_eps, double* grad_inlet) {
+                                    const float* Pd, double* grad_eps, double* grad_inlet) {
   Geo g = make_geo(p);
   const long long n = g.n;
   std::vector<double> gi_acc(POG_INLET_NCOEF, 0.0);
@@ -1016,7 +1108,10 @@ extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint32_t* flags, 
             coef[kk] = Dual((double)p->inlet_coef[kk]);
             coef[kk].d[20 + kk] = 1.0;
           }
-          collide<Dual>(p, g, fl, i, j, k, f, nullptr, nullptr, eps != nullptr, e, Dual(0.0), fs,
+          Dual pd[4];
+          if (Pd)
+            for (int a = 0; a < 4; ++a) pd[a] = Dual((double)Pd[a * n + c]);
+          collide<Dual>(p, g, fl, i, j, k, f, nullptr, Pd ? pd : nullptr, eps != nullptr, e, Dual(0.0), fs,
                         rho, u, nullptr, coef);
           for (int q = 0; q < 19; ++q) {
             double acc = 0;

@@ -2,7 +2,8 @@
 the filter band and the 16 radial inlet-profile coefficients.
 
 Forward: T natural-layout push steps (pog_step_push) from equilibrium, J = sum_t outflow_t
-(FP64 device reduction), with the state checkpointed every K steps.  Backward: for each
+(pog_outflow_fixed: an order-independent fixed-point sum, so J repeats bit for bit), with the
+state checkpointed every K steps.  Backward: for each
 segment, last first, the K states are recomputed from the checkpoint and the hand-written
 adjoint kernel (pog_adjoint_step) runs back through them; parameter gradients accumulate in
 FP64.  Memory: T/K checkpoints + K states.  `OutflowLoss` exposes this as a
@@ -13,11 +14,11 @@ The reference has no differentiable path (no Taichi autodiff on it); this is new
 import dataclasses
 from typing import Optional
 
+import numpy as np
 import torch
 
 from . import _lib
-from .params import (INLET_NCOEF, RED_COUNT, RED_OUTFLOW, STORE_F32, STORE_F64,
-                     LatticeConfig)
+from .params import INLET_NCOEF, STORE_F32, STORE_F64, LatticeConfig
 
 _DT = {STORE_F32: torch.float32, STORE_F64: torch.float64}
 
@@ -30,7 +31,19 @@ class AdjointResult:
 
 
 class OutflowAdjoint:
-    def __init__(self, cfg: LatticeConfig, steps: int, checkpoint_every: int, device="cuda"):
+    """J and its gradients for a lattice run of `steps` steps, checkpointed every
+    `checkpoint_every` steps.
+
+    particles (ParticleConfig, optional): the run is two-way coupled as
+    GB300LBMSolver.step_with_two_way_coupling (legacy/lbm_solver.py:1485-1509): before step t a
+    coupling pass moves the particles in the velocity the previous step computed (zero before the
+    first step) and deposits their drag (Kp, Kv), which step t reads.  The deposit is recorded per
+    step (deterministic fixed-point mode) and enters the adjoint as a fixed input of its step: the
+    gradient is that of J with the particles' forcing held at its recorded history.  `loss_frozen`
+    evaluates J under that same recorded forcing, which is what finite differences of these
+    gradients compare against."""
+
+    def __init__(self, cfg: LatticeConfig, steps: int, checkpoint_every: int, device="cuda", particles=None):
         if cfg.storage not in _DT:
             raise ValueError("the adjoint runs on FP32 or FP64 storage")
         self.lib = _lib.load()
@@ -50,28 +63,59 @@ class OutflowAdjoint:
                       for _ in range(self.nseg)]
         self._states = [torch.empty((19,) + shape, dtype=self.dtype, device=self.device)
                         for _ in range(self.K)]
-        self._red = torch.zeros(RED_COUNT, dtype=torch.float64, device=self.device)
+        # J in fixed point (units of 2^-48): the same bits on every run
+        self._jfix = torch.zeros(1, dtype=torch.int64, device=self.device)
         self._p = None
         self._eps = None
+        self.pc = particles
+        if particles is not None:
+            self._init_particles(particles)
 
+    # ---- particles -----------------------------------------------------------------------------
+    def _init_particles(self, pc):
+        from .params import seed_particles
+        if pc.count <= 0:
+            raise ValueError("a coupled adjoint needs particles")
+        pc = dataclasses.replace(pc, deterministic=True)  # the recomputed deposits repeat bit for bit
+        self.pc = pc
+        self._pp = pc.to_c()
+        pos, vel, d, act = seed_particles(self.cfg, pc)
+        dev = self.device
+        self._p0 = [torch.as_tensor(a).to(dev) for a in (pos, vel, np.zeros_like(pos), act)]
+        self._d = torch.as_tensor(d).to(dev)
+        self._part = [a.clone() for a in self._p0]  # pos, vel, drag_old, active
+        self._pck = [[a.clone() for a in self._p0] for _ in range(self.nseg)]
+        n = self.cfg.ncell
+        self._u = torch.zeros((3,) + self.shape, dtype=torch.float32, device=dev)
+        self._uck = [torch.zeros_like(self._u) for _ in range(self.nseg)]
+        self._fix = torch.zeros(4 * n, dtype=torch.int64, device=dev)
+        self._deps = [torch.zeros((4,) + self.shape, dtype=torch.float32, device=dev) for _ in range(self.K)]
+        self._dep_hist = None  # all T deposits of the last forward (for loss_frozen), on request
+
+    def _couple(self, u, out):
+        """One coupling pass on the current particle state in velocity u; deposit into out."""
+        pos, vel, drag, act = self._part
+        self._fix.zero_()
+        _lib.check(self.lib.pog_particles_couple(self._p, self._pp, _lib.ptr(pos), _lib.ptr(vel), _lib.ptr(self._d),
+                                                 _lib.ptr(drag), _lib.ptr(act), int(self.pc.count), None,
+                                                 _lib.ptr(u), None, _lib.ptr(self._fix), None, _lib.stream_handle()))
+        _lib.check(self.lib.pog_drag_from_fixed(self._p, _lib.ptr(self._fix), _lib.ptr(out), _lib.stream_handle()))
+
+    # ---- steps ---------------------------------------------------------------------------------
     def _params(self, coef):
         c = self.cfg.replace(inlet_coef=tuple(float(x) for x in coef))
         return c.to_c()
 
-    def _push(self, fin, fout, red=None):
+    def _push(self, fin, fout, pdrag=None, u_out=None):
         _lib.check(self.lib.pog_step_push(self._p, _lib.ptr(fin), _lib.ptr(fout), _lib.ptr(self.flags),
-                                          None, None, _lib.ptr(self._eps), None, None, None,
-                                          _lib.ptr(red), _lib.stream_handle()))
+                                          None, _lib.ptr(pdrag), _lib.ptr(self._eps), None, None, _lib.ptr(u_out),
+                                          None, _lib.stream_handle()))
 
-    def forward(self, porosity: Optional[torch.Tensor], inlet_coef, initial: Optional[torch.Tensor] = None) -> float:
-        """Run the forward pass, keep checkpoints, return J.  initial: plain distributions f_q in
-        natural layout [19, NZ, NY, NX], float32 or float64 on the device (pog_export_natural's
-        output), the T steps start from (default: equilibrium at rest)."""
+    def _start(self, porosity, inlet_coef, initial):
         self._p = self._params(inlet_coef)
         self._eps = None if porosity is None else porosity.to(self.device, torch.float32).contiguous().reshape(self.shape)
         s = _lib.stream_handle()
         cur = self._states[0]
-        nxt = self._states[1] if self.K > 1 else torch.empty_like(cur)
         if initial is None:
             _lib.check(self.lib.pog_init_equilibrium(self._p, _lib.ptr(cur), _lib.ptr(self.flags),
                                                      float(self.cfg.rho0), 0.0, 0.0, 0.0, s))
@@ -82,13 +126,59 @@ class OutflowAdjoint:
             in_store = STORE_F32 if src.dtype == torch.float32 else STORE_F64
             _lib.check(self.lib.pog_import_natural(self._p, _lib.ptr(src), in_store, _lib.ptr(self.flags),
                                                    _lib.ptr(cur), s))
-        self._red.zero_()
+        self._jfix.zero_()
+        return cur
+
+    def forward(self, porosity: Optional[torch.Tensor], inlet_coef, initial: Optional[torch.Tensor] = None,
+                record_deposits: bool = False) -> float:
+        """Run the forward pass, keep checkpoints, return J.  initial: plain distributions f_q in
+        natural layout [19, NZ, NY, NX], float32 or float64 on the device (pog_export_natural's
+        output), the T steps start from (default: equilibrium at rest).  With particles,
+        record_deposits keeps all T deposits for loss_frozen."""
+        cur = self._start(porosity, inlet_coef, initial)
+        s = _lib.stream_handle()
+        nxt = self._states[1] if self.K > 1 else torch.empty_like(cur)
+        if self.pc is not None:
+            for a, b in zip(self._part, self._p0):
+                a.copy_(b)
+            self._u.zero_()
+            if record_deposits:
+                self._dep_hist = [torch.empty((4,) + self.shape, dtype=torch.float32, device=self.device)
+                                  for _ in range(self.T)]
+        dep = self._deps[0] if self.pc is not None else None
         for t in range(self.T):
             if t % self.K == 0:
-                self._ckpt[t // self.K].copy_(cur)
-            self._push(cur, nxt, self._red)
+                seg = t // self.K
+                self._ckpt[seg].copy_(cur)
+                if self.pc is not None:
+                    self._uck[seg].copy_(self._u)
+                    for a, b in zip(self._pck[seg], self._part):
+                        a.copy_(b)
+            _lib.check(self.lib.pog_outflow_fixed(self._p, _lib.ptr(cur), _lib.ptr(self.flags), _lib.ptr(self._jfix), s))
+            if self.pc is not None:
+                self._couple(self._u, dep)
+                if record_deposits:
+                    self._dep_hist[t].copy_(dep)
+            self._push(cur, nxt, dep, self._u if self.pc is not None else None)
             cur, nxt = nxt, cur
-        return float(self._red[RED_OUTFLOW])
+        return self._loss()
+
+    def loss_frozen(self, porosity: Optional[torch.Tensor], inlet_coef) -> float:
+        """J with the particles' deposits held at those recorded by the last
+        forward(..., record_deposits=True): the function the coupled adjoint differentiates."""
+        if self.pc is None or self._dep_hist is None:
+            raise RuntimeError("loss_frozen needs a forward(..., record_deposits=True) with particles")
+        cur = self._start(porosity, inlet_coef, None)
+        s = _lib.stream_handle()
+        nxt = self._states[1] if self.K > 1 else torch.empty_like(cur)
+        for t in range(self.T):
+            _lib.check(self.lib.pog_outflow_fixed(self._p, _lib.ptr(cur), _lib.ptr(self.flags), _lib.ptr(self._jfix), s))
+            self._push(cur, nxt, self._dep_hist[t])
+            cur, nxt = nxt, cur
+        return self._loss()
+
+    def _loss(self) -> float:
+        return float(self._jfix.item()) * 2.0 ** -48
 
     def backward(self, want_porosity_grad: bool = True) -> AdjointResult:
         s = _lib.stream_handle()
@@ -101,14 +191,25 @@ class OutflowAdjoint:
             t0 = seg * self.K
             t1 = min(self.T, t0 + self.K)
             self._states[0].copy_(self._ckpt[seg])
-            for i in range(t1 - t0 - 1):
-                self._push(self._states[i], self._states[i + 1])
+            if self.pc is not None:
+                # recompute the segment's coupled steps: the same deposits as the forward pass
+                self._u.copy_(self._uck[seg])
+                for a, b in zip(self._part, self._pck[seg]):
+                    a.copy_(b)
+                for i in range(t1 - t0):
+                    self._couple(self._u, self._deps[i])
+                    if i + 1 < t1 - t0:
+                        self._push(self._states[i], self._states[i + 1], self._deps[i], self._u)
+            else:
+                for i in range(t1 - t0 - 1):
+                    self._push(self._states[i], self._states[i + 1])
             for t in reversed(range(t0, t1)):
+                dep = self._deps[t - t0] if self.pc is not None else None
                 _lib.check(self.lib.pog_adjoint_step(
                     self._p, _lib.ptr(self._states[t - t0]), _lib.ptr(lam_next), _lib.ptr(lam_t),
-                    _lib.ptr(self.flags), _lib.ptr(self._eps), _lib.ptr(g_eps), _lib.ptr(g_in), s))
+                    _lib.ptr(self.flags), _lib.ptr(self._eps), _lib.ptr(dep), _lib.ptr(g_eps), _lib.ptr(g_in), s))
                 lam_next, lam_t = lam_t, lam_next
-        return AdjointResult(float(self._red[RED_OUTFLOW]), g_eps, g_in)
+        return AdjointResult(self._loss(), g_eps, g_in)
 
     def loss(self, porosity: Optional[torch.Tensor], inlet_coef) -> float:
         """Forward only (for finite differences)."""

@@ -14,7 +14,8 @@
 //   3. adds dflux_t/df = -c_z on outlet cells (J = sum_t outflow flux);
 //   4. accumulates dJ/deps (per cell) and dJ/da_k (inlet profile) in FP64.
 // Supported forward configuration: LES off or LOCAL, drag SEMI_IMPLICIT, Guo forcing, no tau
-// clamp, no external force field.  Gated LES cells (|S| below the floor, nu at its cap) and
+// clamp, no external force field; a particle drag deposit (Kp, Kv) enters as a fixed input of
+// the step (its force Kv - Kp u is differentiated through u, the deposit itself is held).  Gated LES cells (|S| below the floor, nu at its cap) and
 // |u| = 0 points take the zero subgradient.
 #include "collide.cuh"
 
@@ -155,7 +156,7 @@ template <int S>
 __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
-    const uint32_t* __restrict__ flags, const float* __restrict__ eps,
+    const uint32_t* __restrict__ flags, const float* __restrict__ eps, const float* __restrict__ pdrag,
     double* __restrict__ grad_eps, double* __restrict__ grad_inlet, uint32_t inlet_lo, uint32_t inlet_hi) {
   using St = Store<S>;
   using C = typename St::C;
@@ -214,9 +215,21 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
         bf[q] = brho + (C)cx(q) * bmx + (C)cy(q) * bmy + (C)cz(q) * bmz - (C)cz(q);  // + dflux/df
     } else {
       // ---- forward recomputation ----
+      // particle drag deposit (Kp, Kv) of this step, a fixed input: the fluid force Kv - Kp u
+      // with u implicit (collide_cell), A = 1 + Kp / (2 rho)
+      C Kp = 0, Kvx = 0, Kvy = 0, Kvz = 0;
+      if (pdrag) {
+        Kp = (C)pdrag[c];
+        Kvx = (C)pdrag[n + c];
+        Kvy = (C)pdrag[2u * n + c];
+        Kvz = (C)pdrag[3u * n + c];
+      }
+      const C Ap = (C)1 + (C)0.5 * Kp / rho;
       const C Gx = rho * (C)kp.gx, Gy = rho * (C)kp.gy, Gz = rho * (C)kp.gz;
-      const C vx = (mx + (C)0.5 * Gx) / rho, vy = (my + (C)0.5 * Gy) / rho, vz = (mz + (C)0.5 * Gz) / rho;
-      C ux = vx, uy = vy, uz = vz, Fx = Gx, Fy = Gy, Fz = Gz;
+      const C vx = (mx + (C)0.5 * (Gx + Kvx)) / rho, vy = (my + (C)0.5 * (Gy + Kvy)) / rho,
+              vz = (mz + (C)0.5 * (Gz + Kvz)) / rho;
+      C ux = vx / Ap, uy = vy / Ap, uz = vz / Ap;
+      C Fx = Gx + Kvx - Kp * ux, Fy = Gy + Kvy - Kp * uy, Fz = Gz + Kvz - Kp * uz;
       const bool porous = (fl & POG_CELL_POROUS) != 0;
       C K = (C)kp.K0, CF = (C)kp.CF0, e = (C)kp.eps0;
       C sK = 0, c0 = 0, c1 = 0, vm = 0, Ed = 0, D = 0, s = 0, um = 0, a = 0, b = 0, coef = 0;
@@ -230,7 +243,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
           CF = (C)kp.CF0 * (rr * sqrt(rr));
         }
         sK = sqrt(K);
-        c0 = (C)0.5 * ((C)1 + (C)0.5 * nu0 / K);
+        c0 = (C)0.5 * (Ap + (C)0.5 * nu0 / K);
         c1 = (C)0.5 * CF / sK;
         vm = sqrt(vx * vx + vy * vy + vz * vz);
         Ed = sqrt(c0 * c0 + c1 * vm);
@@ -243,9 +256,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
         a = nu0 / K;
         b = CF / sK;
         coef = rho * (a + b * um);
-        Fx = Gx - coef * ux;
-        Fy = Gy - coef * uy;
-        Fz = Gz - coef * uz;
+        Fx = Gx + Kvx - (coef + Kp) * ux;
+        Fy = Gy + Kvy - (coef + Kp) * uy;
+        Fz = Gz + Kvz - (coef + Kp) * uz;
       }
       // f becomes f - f_eq in place (f itself is not needed again)
       C* const neq = f;
@@ -339,15 +352,15 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
         buy += by;
         buz += bz;
       }
-      C bvx, bvy, bvz, bGx, bGy, bGz;
+      C bvx, bvy, bvz, bGx, bGy, bGz, bAp = 0;
       if (porous) {
         bGx = bFx;
         bGy = bFy;
         bGz = bFz;
         const C bcoef = -(bFx * ux + bFy * uy + bFz * uz);
-        bux += -coef * bFx;
-        buy += -coef * bFy;
-        buz += -coef * bFz;
+        bux += -(coef + Kp) * bFx;
+        buy += -(coef + Kp) * bFy;
+        buz += -(coef + Kp) * bFz;
         brho += bcoef * (a + b * um);
         const C bum = bcoef * rho * b;
         const C ba = bcoef * rho;
@@ -363,6 +376,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
         bvz = s * buz;
         const C bD = -bs / (D * D);
         const C bc0 = bD * ((C)1 + c0 / Ed);
+        bAp += (C)0.5 * bc0;
         const C bc1 = bD * vm / ((C)2 * Ed);
         const C bvm = bD * c1 / ((C)2 * Ed);
         if (vm > (C)0) {
@@ -379,14 +393,21 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
           grad_eps[c] += (double)(bK * dK + bCF * dCF);
         }
       } else {
-        bvx = bux;
-        bvy = buy;
-        bvz = buz;
+        // F = G + Kv - Kp u, u = v / Ap
+        bux += -Kp * bFx;
+        buy += -Kp * bFy;
+        buz += -Kp * bFz;
+        bvx = bux / Ap;
+        bvy = buy / Ap;
+        bvz = buz / Ap;
+        bAp = -(bux * ux + buy * uy + buz * uz) / Ap;
         bGx = bFx;
         bGy = bFy;
         bGz = bFz;
       }
-      // v = (m + G/2)/rho, G = rho g
+      // Ap = 1 + Kp / (2 rho)
+      brho += bAp * ((C)-0.5 * Kp / (rho * rho));
+      // v = (m + (G + Kv)/2)/rho, G = rho g
       bmx = bvx / rho;
       bmy = bvy / rho;
       bmz = bvz / rho;
@@ -411,7 +432,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
 
 template <int S>
 static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* lt, const uint32_t* flags,
-                      const float* eps, double* ge, double* gi, cudaStream_t s) {
+                      const float* eps, const float* pdrag, double* ge, double* gi, cudaStream_t s) {
   auto kern = adjoint_kernel<S>;
   static thread_local int grid = 0;
   if (grid == 0) grid = persistent_blocks((const void*)kern, ADJ_BLOCK);
@@ -420,7 +441,7 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
   int g = want < grid ? want : grid;
   using E = typename Store<S>::E;
   const uint32_t lo = (kp.nz - 2u) * kp.nxny, hi = lo + kp.nxny;  // the inlet plane
-  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, ge, gi, lo, hi);
+  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, pdrag, ge, gi, lo, hi);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   adjoint_inlet_kernel<S><<<1, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi, gi);
@@ -429,12 +450,56 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
   return POG_OK;
 }
 
+// Outflow flux of a natural-layout state, -sum over outlet cells of sum_q c_qz f_q, added to an
+// int64 accumulator in units of 2^-48 per cell: integer addition is associative, so the total does
+// not depend on the order in which blocks arrive and repeated runs agree bit for bit.
+constexpr double OUTFLOW_FIX_SCALE = 281474976710656.0;  // 2^48
+
+template <int S>
+__global__ void outflow_fixed_kernel(const KParams kp, const typename Store<S>::E* __restrict__ f,
+                                     const uint32_t* __restrict__ flags, unsigned long long* __restrict__ acc) {
+  using St = Store<S>;
+  using C = typename St::C;
+  const uint32_t n = kp.n;
+  long long part = 0;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const uint32_t fl = flags[c];
+    if (!(fl & POG_CELL_OUTLET) || (fl & POG_CELL_SOLID)) continue;
+    C mz = 0;
+#pragma unroll
+    for (int q = 0; q < 19; ++q)
+      if (cz(q) != 0) mz += (C)cz(q) * St::ld(f, (uint32_t)q * n + c, q, (C)kp.rho0);
+    part += __double2ll_rn(-(double)mz * OUTFLOW_FIX_SCALE);
+  }
+  if (part != 0) atomicAdd(acc, (unsigned long long)part);
+}
+
 }  // namespace pog
 
 using namespace pog;
 
+extern "C" int pog_outflow_fixed(const pog_params* p, const void* f_nat, const uint32_t* flags,
+                                 long long* acc, void* stream) {
+  int rc = pog_validate_params(p);
+  if (rc) return rc;
+  if (!f_nat || !flags || !acc) return set_error(POG_E_ARG, "NULL pointer");
+  KParams kp = make_kparams(p);
+  cudaStream_t s = (cudaStream_t)stream;
+  long long want = ((long long)kp.n + 255) / 256;
+  const int grid = (int)(want < 152 * 8 ? want : 152 * 8);
+  if (p->storage == POG_STORE_F32)
+    outflow_fixed_kernel<POG_STORE_F32><<<grid, 256, 0, s>>>(kp, (const float*)f_nat, flags, (unsigned long long*)acc);
+  else if (p->storage == POG_STORE_F64)
+    outflow_fixed_kernel<POG_STORE_F64><<<grid, 256, 0, s>>>(kp, (const double*)f_nat, flags, (unsigned long long*)acc);
+  else
+    return set_error(POG_E_ARG, "pog_outflow_fixed reads F32 or F64 natural-layout states");
+  count_launch();
+  POG_TRY_CUDA(cudaGetLastError());
+  return POG_OK;
+}
+
 extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next,
-                                void* lam_t, const uint32_t* flags, const float* porosity,
+                                void* lam_t, const uint32_t* flags, const float* porosity, const float* pdrag,
                                 double* grad_porosity, double* grad_inlet, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
@@ -450,8 +515,8 @@ extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void
   KParams kp = make_kparams(p);
   cudaStream_t s = (cudaStream_t)stream;
   if (p->storage == POG_STORE_F32)
-    return launch_adj<POG_STORE_F32>(kp, f_t, lam_next, lam_t, flags, porosity, grad_porosity, grad_inlet, s);
+    return launch_adj<POG_STORE_F32>(kp, f_t, lam_next, lam_t, flags, porosity, pdrag, grad_porosity, grad_inlet, s);
   if (p->storage == POG_STORE_F64)
-    return launch_adj<POG_STORE_F64>(kp, f_t, lam_next, lam_t, flags, porosity, grad_porosity, grad_inlet, s);
+    return launch_adj<POG_STORE_F64>(kp, f_t, lam_next, lam_t, flags, porosity, pdrag, grad_porosity, grad_inlet, s);
   return set_error(POG_E_ARG, "adjoint storage must be F32 or F64");
 }

@@ -141,3 +141,84 @@ def test_forward_from_a_given_state(cuda):
     run.forward(eps, cfg.inlet_coef, initial=nat)
     r = run.backward()
     assert torch.isfinite(r.grad_porosity).all() and r.grad_porosity.abs().max() > 0
+
+
+def _coupled_case():
+    from pour_over_coffee_lbm_gb300.params import ParticleConfig
+    cfg = _case().replace(storage=STORE_F64, nx=20, ny=20, nz=24, cone_apex_z=3.0, inlet_radius=5.0)
+    # heavy enough particles for their drag to matter in a short run
+    pc = ParticleConfig(count=400, density_ratio=1.5, median_diameter=0.9, seed=77)
+    return cfg, pc
+
+
+def test_coupled_adjoint_matches_dual_number_oracle(cuda, orc):
+    """With particles: the GPU adjoint (deposits recorded per step, held fixed) equals the oracle's
+    dual-number adjoint through the same deposits and its own FP64 forward states."""
+    cfg, pc = _coupled_case()
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps_np = porosity_field(cfg, fl, seed=21)
+    eps = torch.as_tensor(eps_np).reshape(cfg.nz, cfg.ny, cfg.nx)
+    T = 12
+    run = OutflowAdjoint(cfg, steps=T, checkpoint_every=5, particles=pc)
+    J = run.forward(eps, cfg.inlet_coef, record_deposits=True)
+    res = run.backward()
+    deps = [d.cpu().numpy() for d in run._dep_hist]
+    assert max(float(np.abs(d[0]).max()) for d in deps) > 0  # the particles deposited drag
+    assert run.loss_frozen(eps, cfg.inlet_coef) == J  # the recorded forcing reproduces J bit for bit
+    # oracle: forward states under the recorded deposits, then the dual-number adjoint back
+    f = orc.init_equilibrium(cfg, fl, np.float64)
+    states = []
+    for t in range(T):
+        states.append(f)
+        f, _, _ = orc.step(cfg, fl, f, eps=eps_np.reshape(cfg.nz, cfg.ny, cfg.nx), pdrag=deps[t])
+    lam = np.zeros_like(f)
+    ge = np.zeros(cfg.ncell)
+    gi = np.zeros(16)
+    for t in reversed(range(T)):
+        lam = orc.adjoint_step(cfg, fl, states[t], lam, eps=eps_np, grad_eps=ge, grad_inlet=gi, pdrag=deps[t])
+    g_gpu = res.grad_porosity.cpu().numpy().reshape(-1)
+    assert np.abs(g_gpu - ge).max() <= 1e-7 * np.abs(ge).max()
+    gin = res.grad_inlet.cpu().numpy()
+    assert np.abs(gin - gi).max() <= 1e-7 * np.abs(gi).max()
+    # and the particles change the gradient (the deposit term is live)
+    bare = OutflowAdjoint(cfg, steps=T, checkpoint_every=5)
+    bare.forward(eps, cfg.inlet_coef)
+    rb = bare.backward()
+    assert np.abs(rb.grad_porosity.cpu().numpy().reshape(-1) - g_gpu).max() > 1e-6 * np.abs(g_gpu).max()
+
+
+def test_coupled_adjoint_finite_differences(cuda):
+    """Central differences (h = 1e-3) of J under the recorded particle forcing."""
+    cfg, pc = _coupled_case()
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=23)).reshape(cfg.nz, cfg.ny, cfg.nx)
+    run = OutflowAdjoint(cfg, steps=40, checkpoint_every=10, particles=pc)
+    run.forward(eps, cfg.inlet_coef, record_deposits=True)
+    res = run.backward()
+    h = 1e-3
+    coef = np.array(cfg.inlet_coef, np.float64)
+    for k in (0, 2, 7):
+        cp = coef.copy(); cp[k] += h
+        cm = coef.copy(); cm[k] -= h
+        fd = (run.loss_frozen(eps, cp) - run.loss_frozen(eps, cm)) / (2 * h)
+        ad = res.grad_inlet[k].item()
+        assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-14, (k, ad, fd)
+    ge = res.grad_porosity.cpu().numpy().reshape(-1)
+    band = np.flatnonzero((fl.reshape(-1) & CELL_POROUS) != 0)
+    flat = eps.reshape(-1)
+    for c in band[np.argsort(-np.abs(ge[band]))[:6]]:
+        ep = flat.clone(); ep[c] += h
+        em = flat.clone(); em[c] -= h
+        hh = (ep[c].double() - em[c].double()).item() / 2
+        fd = (run.loss_frozen(ep.reshape(eps.shape), coef) - run.loss_frozen(em.reshape(eps.shape), coef)) / (2 * hh)
+        assert abs(ge[c] - fd) <= 1e-4 * abs(fd), (c, ge[c], fd)
+
+
+def test_loss_repeats_bit_for_bit(cuda):
+    """J is an order-independent fixed-point sum: repeated forward runs give the same bits."""
+    cfg = _case().replace(storage=STORE_F64, nx=24, ny=24, nz=24)
+    run = OutflowAdjoint(cfg, steps=30, checkpoint_every=10)
+    js = {run.forward(None, cfg.inlet_coef) for _ in range(3)}
+    assert len(js) == 1 and next(iter(js)) != 0.0
