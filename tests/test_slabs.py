@@ -119,3 +119,70 @@ def test_slab_helpers():
                 jj, ii = j - cy, i - cx
                 inside = 0 <= jj < 4 and 0 <= ii < 5
                 assert m[a, j, i] == (inside and not (jj == 1 and ii == 2))
+
+
+# ---- the same protocol driving the oracle's restatement of the product's AA step -------------------
+def _v60_case():
+    from pour_over_coffee_lbm_gb300.params import LES_LOCAL, STORE_F64, LatticeConfig
+    # a V60 lattice with flow through the slab interfaces: inlet jet, LES, porous band, gravity
+    return LatticeConfig(nx=20, ny=18, nz=24, band_thickness=2.0, les_mode=LES_LOCAL, u_inlet=-0.05,
+                         cs_smag=0.3, storage=STORE_F64)
+
+
+ORC_STEPS = 17
+
+
+def _rank_oracle(rank, world, port, outdir):
+    import oracle
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    cfg = _v60_case()
+    flags = oracle.build_flags(cfg)
+    f = oracle.init_equilibrium(cfg, flags, np.float64)
+    z0, z1 = slab_bounds(cfg.nz, world)[rank]
+    fl = slab_flags(flags, z0, z1)
+    fs = np.zeros((19, z1 - z0 + 2, cfg.ny, cfg.nx))
+    lo, hi = max(z0 - 1, 0), min(z1 + 1, cfg.nz)
+    fs[:, lo - (z0 - 1): hi - (z0 - 1)] = f[:, lo:hi]
+    ft = torch.from_numpy(fs)  # shares memory with fs
+    halo = RankHalo(fl, rank, world)
+    scfg = cfg.replace(nz=z1 - z0 + 2)
+    for t in range(ORC_STEPS):
+        if t % 2:
+            halo.exchange_in(ft)
+        oracle.step_aa(scfg, fl, fs, t)
+        if t % 2:
+            halo.exchange_out(ft)
+    if ORC_STEPS % 2:
+        halo.exchange_in(ft)
+    np.save(os.path.join(outdir, "oslab%d.npy" % rank), fs)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_rank_halo_with_the_oracle_aa_step(tmp_path, world):
+    """gloo ranks each step their z-slab with the oracle's AA step (the product's stepping order and
+    collision) through RankHalo; the assembled state equals the undivided oracle AA run and the
+    oracle's push run bit for bit."""
+    import oracle
+    cfg = _v60_case()
+    flags = oracle.build_flags(cfg)
+    f0 = oracle.init_equilibrium(cfg, flags, np.float64)
+    aa = f0.copy()
+    push = f0.copy()
+    for t in range(ORC_STEPS):
+        oracle.step_aa(cfg, flags, aa, t)
+        push, _, _ = oracle.step(cfg, flags, push)
+    ref = _natural(aa, flags, ORC_STEPS)
+    fluid = (flags & 1) == 0
+    inner = np.zeros(flags.shape, bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    live = fluid & inner
+    assert np.array_equal(ref[:, live], push[:, live])  # AA order == push order, bit for bit
+    mp.start_processes(_rank_oracle, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    got = np.zeros_like(f0)
+    for r, (z0, z1) in enumerate(slab_bounds(cfg.nz, world)):
+        fs = np.load(tmp_path / ("oslab%d.npy" % r))
+        got[:, z0:z1] = _natural(fs, slab_flags(flags, z0, z1), ORC_STEPS)[:, 1:-1]
+    assert np.array_equal(got[:, live], ref[:, live])
+    assert np.abs(ref[:, live] - f0[:, live]).max() > 1e-4  # the state did evolve
