@@ -5,8 +5,15 @@
 // memory budget and forbids any further device allocation once it is running (its own memory
 // manager owns the GPU), or a loop that must never block on, or fail in, an allocator.  For them,
 // pog_particles_bin_noalloc runs the same binning and sort with its scratch in a device array
-// that is part of this library's image: it is reserved when the library is loaded on a GPU and
-// stays reserved on every GPU that loaded it until the process exits.
+// that is part of this library's image.  CUDA loads a library's device code lazily, per device:
+// the 20 MiB array is reserved on a GPU by the first call on that GPU (which also resolves its
+// address) and stays reserved there until the process exits.  A caller with a fixed memory budget
+// therefore makes one call with np = 0 on each device at set-up time -- before its budget is fixed
+// and before any stream capture -- and then never allocates again.
+//
+// The address is resolved once per device ordinal and cached.  The current device must be the
+// device of `stream`, and the cache does not survive cudaDeviceReset (the device's code and its
+// array are reloaded at a new address): do not use this entry point across a reset.
 //
 // Limit: POG_NOALLOC_MAX_PARTICLES particles (the array is sized for exactly that many).
 // The array is shared by every call on a device and keeps the previous call's contents; the

@@ -2,9 +2,9 @@
 pour_over_coffee_lbm_gb300 mirrors (lattice and multiphase parameters, the physical scales of the
 diagnostics and the analysis export), read by importing the reference's own `config` package.
 
-    python tests/golden/make_config_golden.py [path of the reference checkout]
+    python tests/golden/make_config_golden.py <path of the reference checkout>
 
-Runs only where the reference checkout exists (default /root/reference); the JSON travels with
+Runs only where the reference checkout exists (its path is the script's required first argument); the JSON travels with
 the tests (tests/test_reference_config.py).
 """
 import json
@@ -18,7 +18,7 @@ NAMES = ["NX", "NY", "NZ", "TAU_WATER", "TAU_AIR", "SMAGORINSKY_CONSTANT", "RHO_
 
 
 def main():
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     import config  # the reference's config package
     out = {k: getattr(config, k) for k in NAMES}
     with open(os.path.join(HERE, "reference_config.json"), "w") as f:
@@ -27,4 +27,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_config_golden.py <path of the reference checkout>")
     main()

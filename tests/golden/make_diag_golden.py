@@ -2,9 +2,9 @@
 (src/visualization/lbm_diagnostics.py, plain numpy, importable without Taichi) run on seeded
 synthetic fields.
 
-    python tests/golden/make_diag_golden.py [path of the reference checkout]
+    python tests/golden/make_diag_golden.py <path of the reference checkout>
 
-The script imports the reference from its checkout (default /root/reference), so it runs only
+The script imports the reference from its checkout (its path is the script's required first argument), so it runs only
 where that checkout exists; the fixtures it writes travel with the tests.  The reference reads its
 grid size, gravity and scales from its `config` package.  Its NX/NY/NZ (the region split of
 detailed_flow_analysis and the particles' radial centre) are set to the fixture's grid, and
@@ -83,7 +83,7 @@ def clean(d):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1]
     sys.path.insert(0, ref)
     import config  # the reference's config package
     config.NX, config.NY, config.NZ = SHAPE
@@ -107,4 +107,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_diag_golden.py <path of the reference checkout>")
     main()

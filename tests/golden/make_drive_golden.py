@@ -2,9 +2,9 @@
 (src/physics/pressure_gradient_drive.py).  Its kernel source runs in this container through
 taichi_standin.py, serially and in float32.
 
-    python tests/golden/make_drive_golden.py [path of the reference checkout]
+    python tests/golden/make_drive_golden.py <path of the reference checkout>
 
-The script runs only where the reference checkout exists (default /root/reference).  The fixture
+The script runs only where the reference checkout exists (its path is the script's required first argument).  The fixture
 travels with tests/test_drive_oracle.py.
 
 Grid: 12 x 10 x 14 (config.NX/NY/NZ set before construction), about 10 % solid cells, seeded
@@ -28,7 +28,7 @@ def main():
     sys.path.insert(0, HERE)
     import taichi_standin
     ti = taichi_standin.install()
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     import config  # the reference's config package
     config.NX, config.NY, config.NZ = SHAPE
     from src.physics.pressure_gradient_drive import PressureGradientDrive
@@ -73,4 +73,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_drive_golden.py <path of the reference checkout>")
     main()

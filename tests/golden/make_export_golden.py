@@ -2,9 +2,9 @@
 reference's own EnhancedVisualizer (src/visualization/enhanced_visualizer.py:1487-1560), run on
 seeded stub fields, plus the inputs it was given.
 
-    python tests/golden/make_export_golden.py [path of the reference checkout]
+    python tests/golden/make_export_golden.py <path of the reference checkout>
 
-The script runs only where the reference checkout exists (default /root/reference).  The fixture
+The script runs only where the reference checkout exists (its path is the script's required first argument).  The fixture
 travels with the tests (tests/test_export.py).
 
 The visualiser module imports matplotlib at the top but does not use it on this path; an empty
@@ -73,7 +73,7 @@ def inputs(seed=7):
 
 
 def main():
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     for name in ("matplotlib", "matplotlib.pyplot", "matplotlib.colors", "matplotlib.patches", "matplotlib.gridspec"):
         sys.modules.setdefault(name, _Stub(name))
     import config  # the reference's config package
@@ -107,4 +107,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_export_golden.py <path of the reference checkout>")
     main()

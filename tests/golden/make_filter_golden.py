@@ -3,9 +3,9 @@
 :702-746).  Their source runs in this container through taichi_standin.py, serially and in
 float32.
 
-    python tests/golden/make_filter_golden.py [path of the reference checkout]
+    python tests/golden/make_filter_golden.py <path of the reference checkout>
 
-The script runs only where the reference checkout exists (default /root/reference).  The fixture
+The script runs only where the reference checkout exists (its path is the script's required first argument).  The fixture
 travels with tests/test_filter_oracle.py.
 
 The kernels read only the paper mask and the two dynamic fields, so the object is made without
@@ -29,7 +29,7 @@ def main():
     sys.path.insert(0, HERE)
     import taichi_standin
     ti = taichi_standin.install()
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     import config  # the reference's config package
     config.NX, config.NY, config.NZ = SHAPE
     from src.physics.filter_paper import FilterPaperSystem
@@ -71,4 +71,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_filter_golden.py <path of the reference checkout>")
     main()

@@ -2,9 +2,9 @@
 (src/core/multiphase_3d.py).  Their source runs in this container through taichi_standin.py,
 serially and in float32.
 
-    python tests/golden/make_multiphase_golden.py [path of the reference checkout]
+    python tests/golden/make_multiphase_golden.py <path of the reference checkout>
 
-The script runs only where the reference checkout exists (default /root/reference).  The fixture
+The script runs only where the reference checkout exists (its path is the script's required first argument).  The fixture
 travels with tests/test_multiphase_oracle.py.
 
 Grid: 10 x 9 x 12 (config.NX/NY/NZ set before construction).  The phase field is a drop of water
@@ -32,7 +32,7 @@ def main():
     sys.path.insert(0, HERE)
     import taichi_standin
     ti = taichi_standin.install()
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     import config  # the reference's config package
     config.NX, config.NY, config.NZ = SHAPE
     from src.core.multiphase_3d import MultiphaseFlow3D
@@ -85,4 +85,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_multiphase_golden.py <path of the reference checkout>")
     main()

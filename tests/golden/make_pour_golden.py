@@ -2,9 +2,9 @@
 (src/physics/precise_pouring.py).  Its kernel source runs in this container through
 taichi_standin.py, serially and in float32.
 
-    python tests/golden/make_pour_golden.py [path of the reference checkout]
+    python tests/golden/make_pour_golden.py <path of the reference checkout>
 
-The script runs only where the reference checkout exists (default /root/reference).  The fixture
+The script runs only where the reference checkout exists (its path is the script's required first argument).  The fixture
 travels with tests/test_pour_oracle.py.  The reference reads its grid from `config`, so
 NX = NY = NZ = 24 are set before construction.  Its nozzle then has diameter 8 cells, stream top
 z = 18 and velocity 0.05 lu/ts, which the fixture records.
@@ -32,7 +32,7 @@ def main():
     sys.path.insert(0, HERE)
     import taichi_standin
     ti = taichi_standin.install()
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     import config  # the reference's config package
     config.NX, config.NY, config.NZ = N, N, N
     from src.physics.precise_pouring import PrecisePouringSystem
@@ -92,4 +92,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_pour_golden.py <path of the reference checkout>")
     main()

@@ -4,9 +4,9 @@ interpolation compute_two_way_coupling_forces uses).  It runs on a seeded veloci
 seeded positions, including positions outside the grid that the gather clamps.  The kernel source
 runs in this container through taichi_standin.py, serially and in float32.
 
-    python tests/golden/make_trilinear_golden.py [path of the reference checkout]
+    python tests/golden/make_trilinear_golden.py <path of the reference checkout>
 
-The script runs only where the reference checkout exists (default /root/reference).  The fixture
+The script runs only where the reference checkout exists (its path is the script's required first argument).  The fixture
 travels with tests/test_oracle_kat.py.  The method reads only the particles' positions, so the
 object is made without its constructor (object.__new__).
 """
@@ -24,7 +24,7 @@ def main():
     sys.path.insert(0, HERE)
     import taichi_standin
     ti = taichi_standin.install()
-    sys.path.insert(0, sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, sys.argv[1])
     import config  # the reference's config package
     config.NX, config.NY, config.NZ = SHAPE
     from src.physics.coffee_particles import CoffeeParticleSystem
@@ -43,4 +43,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_trilinear_golden.py <path of the reference checkout>")
     main()
