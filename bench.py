@@ -2,20 +2,22 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Workload (the coupled FP32 case): 128^3 D3Q19, Smagorinsky LES (Cs 0.1, local strain), 3-cell
-porous filter band (eps 0.6, K 1e-3, C_F 0.55), V60 cone with drain hole and inlet disk,
-Guo gravity, 20,000 log-normal particles (median d 0.6 cells, sigma 0.35, density ratio 1.2)
-two-way coupled.  One step = particle coupling (gather/drag/relax/spread/integrate, cell sort
-every 20 steps) + one fused LBM step.  MLUPS = cells x steps / time (all cells, as the
-reference's benchmark_suite.py:129).  Inputs are seeded synthetic (no dataset exists).
+Headline workload (the metric's configuration): 256^3 D3Q19 in FP32 storage -- BGK, Smagorinsky
+LES (Cs 0.1, local strain), Guo gravity, a 3-cell Darcy-Forchheimer filter band (eps 0.6, K 1e-3,
+C_F 0.55), half-way bounce-back on the V60 cone, inlet disk and drain outlet.  MLUPS = cells x
+steps / time (all cells, as the reference's benchmark_suite.py:129).  Inputs are seeded synthetic
+(no dataset exists).
 
-`value` replays CUDA graphs of 20 coupled steps with all state resident in HBM; `e2e` drives
-the public solver API step by step with a host-to-device copy of the pour control (17 floats)
-and a device-to-host copy of the step's FP64 sums every step.  `roofline` times the dominant
-kernel (the fused LBM step with its particle-force read and u write) alone with CUDA events.
-Extra lines: 256^3 FP32 / FP16S / BF16S storage (LES + porous band, no particles).
-The reference arm (--impl reference) times the CPU restatement of the same workload on the
-host cores (the reference itself is Python + Taichi and cannot run here).
+`value` is the median over 5 timed regions of exactly K steps (CUDA graphs of 20 steps, CUDA
+events on the launching stream, all state resident in HBM; the 1.27 GB distribution buffer is far
+larger than L2, so no flush is needed).  `e2e` drives the public solver API step by step with a
+host-to-device copy of the pour control (17 floats) and a device-to-host copy of the step's FP64
+sums every step.  `roofline` divides the step's algorithmic bytes by the same timing.
+Extra lines: FP16S / BF16S storage at 256^3 (both step kernels, errors against an FP64 run), the
+128^3 two-way coupled case with 20,000 particles, the plugin kernels, the 96^3 differentiation
+case and the 320x320x384 / 1M-particle scale case.
+The reference arm (--impl reference) times the CPU restatement of the same workload on the host
+cores (the reference itself is Python + Taichi and cannot run here).
 """
 import argparse
 import json
@@ -49,6 +51,10 @@ def parse():
     ap.add_argument("--precision-only", choices=["fp32", "fp16s", "bf16s"], default=None,
                     help="time only the 256^3 precision case in this storage for --steps steps (profiling)")
     ap.add_argument("--precision-case", choices=["les_band", "plain"], default="les_band")
+    ap.add_argument("--scale-only", action="store_true",
+                    help="run --steps coupled steps of the 320x320x384 / 1M-particle case (profiling)")
+    ap.add_argument("--step-kernel", choices=["rows", "registers"], default="registers",
+                    help="lattice step kernel: row-tiled TMA-staged, or register-staged")
     return ap.parse_args()
 
 
@@ -148,7 +154,7 @@ def time_graph(graph, replays):
     return start.elapsed_time(end) / 1e3
 
 
-def kernel_roofline(cfg, pc, steps, peak):
+def kernel_roofline(cfg, pc, steps, peak, step_kernel="registers"):
     """Average duration of the fused LBM step kernel alone with the arguments it has inside the
     coupled step (the particle drag deposit and its cell mask of a real coupling pass, rho/u
     written), over `steps` graph-replayed launches."""
@@ -156,7 +162,7 @@ def kernel_roofline(cfg, pc, steps, peak):
     from pour_over_coffee_lbm_gb300.params import CELL_SOLID
     from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
-    s = GB300LBMSolver(cfg)
+    s = GB300LBMSolver(cfg, step_kernel=step_kernel)
     ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
     ps.seed()
     for _ in range(6):
@@ -178,7 +184,9 @@ def kernel_roofline(cfg, pc, steps, peak):
     achieved = bytes_per_launch / per_launch / 1e9
     out = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0], "unit": "GB/s",
            "frac": round(achieved / peak[0], 4), "peak_source": peak[1],
-           "kernel": "aa_step_kernel (fused collide-stream, particle drag read at deposit cells, rho/u write)",
+           "kernel": ("rows_step_kernel with its bounce-back mailbox passes" if step_kernel == "rows" else
+                      "aa_step_kernel") + " (fused collide-stream, particle drag read at deposit cells, rho/u write): "
+                                         "one lattice step",
            "kernel_us": round(per_launch * 1e6, 2), "algorithmic_bytes_per_launch": bytes_per_launch,
            "fluid_cells": nf, "deposit_cells": nd, "cells": s.n}
     del s, g, ps
@@ -336,65 +344,69 @@ def plugin_rows(cfg, pc, steps, peak):
 
 
 def differentiation_rows(peak):
-    """96^3 + band with per-cell porosity 0.6 +- 0.05 and the 16-coefficient inlet profile: 500
-    steps forward and the adjoint with checkpoints every 50, FP32 and FP64, timed; FP64 central
-    differences (h = 1e-3) on the 8 porous cells with the largest gradients and all 16
-    coefficients.  The particles of the case are not part of the differentiated step."""
+    """96^3 + band with per-cell porosity 0.6 +- 0.05, the 16-coefficient inlet profile and 5,000
+    two-way coupled particles: 500 steps forward and the adjoint with checkpoints every 50, FP32
+    and FP64, timed.  The particles' drag deposit is recorded per step and held fixed by the
+    adjoint; FP64 central differences (h = 1e-3) of J under that recorded forcing on the 8 porous
+    cells with the largest gradients and all 16 coefficients check it (bar 1e-4 of the largest
+    component).  The differences of the fully coupled J (particles responding) are reported beside
+    them: their gap to the adjoint is the particles' feedback, which the adjoint leaves out."""
     import numpy as np
     import torch
     from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint
     from pour_over_coffee_lbm_gb300.params import (CELL_POROUS, STORE_F32, STORE_F64, differentiation_96,
                                                    porosity_field)
-    cfg, _ = differentiation_96()
+    cfg, pc = differentiation_96()
     T, K = 500, 50
-    out = {"workload": "%dx%dx%d D3Q19 + LES(local) + band, porosity 0.6 +- 0.05, 16-coefficient inlet; "
-                       "J = sum of outflow over %d steps, checkpoints every %d" % (cfg.nx, cfg.ny, cfg.nz, T, K)}
+    out = {"workload": "%dx%dx%d D3Q19 + LES(local) + band, porosity 0.6 +- 0.05, 16-coefficient inlet, %d particles "
+                       "two-way coupled (deposit recorded per step); J = sum of outflow over %d steps, checkpoints "
+                       "every %d" % (cfg.nx, cfg.ny, cfg.nz, pc.count, T, K)}
     res = {}
     for name, st in (("fp32", STORE_F32), ("fp64", STORE_F64)):
         c = cfg.replace(storage=st)
-        run = OutflowAdjoint(c, T, K)
+        run = OutflowAdjoint(c, T, K, particles=pc)
         fl = run.flags.cpu().numpy()
         eps = torch.as_tensor(porosity_field(c, fl, seed=1234)).reshape(c.nz, c.ny, c.nx).cuda()
         run.forward(eps, c.inlet_coef)  # warm-up
         run.backward()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         ev[0].record()
-        J = run.forward(eps, c.inlet_coef)
+        J = run.forward(eps, c.inlet_coef, record_deposits=(st == STORE_F64))
         ev[1].record()
         r = run.backward()
         ev[2].record()
         torch.cuda.synchronize()
         fwd, bwd = ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3
+        gbs = 458 * c.ncell * T / bwd / 1e9
         out[name] = {"forward_ms": round(fwd * 1e3, 2), "backward_ms": round(bwd * 1e3, 2),
-                     "adjoint_mlups": round(c.ncell * T / bwd / 1e6, 1), "loss": J}
+                     "adjoint_mlups": round(c.ncell * T / bwd / 1e6, 1), "loss": J,
+                     "adjoint_roofline": {"achieved_gbs": round(gbs, 1), "frac": round(gbs / peak[0], 4),
+                                          "bytes": "458 B per cell update"}}
         res[name] = (run, eps, fl, r)
     g32, g64 = res["fp32"][3], res["fp64"][3]
-    out["fp32_vs_fp64_grad_rel"] = {
-        "inlet": float((g32.grad_inlet - g64.grad_inlet).norm() / g64.grad_inlet.norm()),
-        "porosity": float((g32.grad_porosity - g64.grad_porosity).norm() / g64.grad_porosity.norm())}
+    rel = {"inlet": float((g32.grad_inlet - g64.grad_inlet).norm() / g64.grad_inlet.norm()),
+           "porosity": float((g32.grad_porosity - g64.grad_porosity).norm() / g64.grad_porosity.norm())}
+    # bars: the FP32 run recomputes its forward states in FP32, whose u resolution limits the porosity
+    # gradient (concentrated in the band) more than the inlet's
+    out["fp32_vs_fp64_grad_rel"] = dict(rel, bars={"inlet": 1e-3, "porosity": 1e-2},
+                                        ok=rel["inlet"] <= 1e-3 and rel["porosity"] <= 1e-2)
     run, eps, fl, r = res["fp64"]
     h = 1e-3
     coef = np.array(cfg.inlet_coef, np.float64)
-    fds, ads = [], []
+    fds, fdc, ads = [], [], []
     for k in range(16):
         cp, cm = coef.copy(), coef.copy()
         cp[k] += h
         cm[k] -= h
-        fds.append((run.loss(eps, cp) - run.loss(eps, cm)) / (2 * h))
+        fds.append((run.loss_frozen(eps, cp) - run.loss_frozen(eps, cm)) / (2 * h))
         ads.append(r.grad_inlet[k].item())
-    fds, ads = np.array(fds), np.array(ads)
-    err_in = float(np.max(np.abs(ads - fds) / np.maximum(np.abs(fds), 1e-30)))
-    err_in_norm = float(np.max(np.abs(ads - fds)) / np.max(np.abs(fds)))
-    # the same differences at h = 1e-2: J varies in the last digits from run to run (FP64 sums
-    # over blocks), so the small coefficients' differences at h = 1e-3 sit at that noise floor
-    fds2 = []
     for k in range(16):
         cp, cm = coef.copy(), coef.copy()
-        cp[k] += 1e-2
-        cm[k] -= 1e-2
-        fds2.append((run.loss(eps, cp) - run.loss(eps, cm)) / 2e-2)
-    fds2 = np.array(fds2)
-    err_in2 = float(np.max(np.abs(ads - fds2)) / np.max(np.abs(fds2)))
+        cp[k] += h
+        cm[k] -= h
+        fdc.append((run.loss(eps, cp) - run.loss(eps, cm)) / (2 * h))
+    fds, fdc, ads = np.array(fds), np.array(fdc), np.array(ads)
+    err_in = float(np.max(np.abs(ads - fds)) / np.max(np.abs(fds)))
     ge = r.grad_porosity.cpu().numpy().reshape(-1)
     band = np.flatnonzero((fl.reshape(-1) & CELL_POROUS) != 0)
     flat = eps.reshape(-1)
@@ -404,50 +416,72 @@ def differentiation_rows(peak):
         ep[c] += h
         em[c] -= h
         hh = (ep[c].double() - em[c].double()).item() / 2
-        fd = (run.loss(ep.reshape(eps.shape), coef) - run.loss(em.reshape(eps.shape), coef)) / (2 * hh)
+        fd = (run.loss_frozen(ep.reshape(eps.shape), coef) - run.loss_frozen(em.reshape(eps.shape), coef)) / (2 * hh)
         err_eps = max(err_eps, abs(ge[c] - fd) / max(abs(fd), 1e-30))
-    out["fd_max_rel_err_fp64"] = {"inlet_16": err_in, "inlet_16_vs_largest": err_in_norm, "porosity_8": err_eps,
-                                  "h": h, "inlet_16_vs_largest_h1e-2": err_in2, "inlet_fd": fds.tolist(),
-                                  "inlet_fd_h1e-2": fds2.tolist(), "inlet_adjoint": ads.tolist()}
+    out["fd_fp64_h1e-3"] = {"inlet_16_vs_largest": err_in, "porosity_8_max_rel": err_eps,
+                            "bar": 1e-4, "ok": err_in <= 1e-4 and err_eps <= 1e-4,
+                            "inlet_fd_recorded_forcing": fds.tolist(), "inlet_adjoint": ads.tolist(),
+                            "inlet_fd_particles_responding": fdc.tolist(),
+                            "particle_feedback_vs_largest": float(np.max(np.abs(fdc - fds)) / np.max(np.abs(fds)))}
     del res, run
     torch.cuda.empty_cache()
     return out
 
 
-def scale_row(steps, adj_steps=200, ckpt=20):
-    """320x320x384 FP16S + LES + band + 1,000,000 particles: `steps` two-way coupled steps
-    (graph-replayed), then the outflow adjoint over the last adj_steps (recomputed in FP32 from the
-    FP16S state, checkpoints every ckpt)."""
+def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="registers"):
+    """320x320x384 FP16S + LES + band + 1,000,000 particles: exactly `steps` two-way coupled steps
+    (4 eager, the rest graph-replayed), then the outflow adjoint over the last adj_steps of them
+    (recomputed in FP32 from the FP16S state exported at step steps - adj_steps, checkpoints every
+    ckpt).  Roofline fractions: the coupled step at 77 B per cell update (FP16S lattice) plus 268 B
+    per particle (gather, drag, integration, deposit), the adjoint at 458 B per cell update (one
+    forward recomputation, the state and the adjoint state read and written)."""
     import torch
+    from pour_over_coffee_lbm_gb300 import _lib
     from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint
     from pour_over_coffee_lbm_gb300.params import STORE_F32, scale_320x384
     from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     cfg, pc = scale_320x384()
-    s = GB300LBMSolver(cfg)
+    s = GB300LBMSolver(cfg, step_kernel=step_kernel)
     ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
     ps.seed()
     for _ in range(4):
         s.step_with_two_way_coupling(ps)
     g = s.capture(GRAPH_STEPS, ps)
-    g.replay()
     torch.cuda.synchronize()
-    n_fwd = max(GRAPH_STEPS, ((steps - adj_steps - 4 - GRAPH_STEPS) // GRAPH_STEPS) * GRAPH_STEPS)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for _ in range(n_fwd // GRAPH_STEPS):
+    split = steps - adj_steps  # the adjoint window starts here
+    before = split - 4
+    reps1, rem1 = divmod(before, GRAPH_STEPS)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record()
+    for _ in range(reps1):
         g.replay()
-    ev1.record()
-    torch.cuda.synchronize()
-    el = ev0.elapsed_time(ev1) / 1e3
-    stable = bool(s.check_stability())
-    del g
+    for _ in range(rem1):
+        s.step_with_two_way_coupling(ps)
+    ev[1].record()
     nat = torch.empty((19, cfg.nz, cfg.ny, cfg.nx), dtype=torch.float32, device="cuda")
-    from pour_over_coffee_lbm_gb300 import _lib
     _lib.check(s.lib.pog_export_natural(s._p, _lib.ptr(s._f), _lib.ptr(s._flags), s.t, _lib.ptr(nat), STORE_F32,
                                         _lib.stream_handle()))
+    ev[2].record()
+    left = adj_steps
+    if s.t % 2:  # graphs replay at even time indices
+        s.step_with_two_way_coupling(ps)
+        left -= 1
+    reps2, rem2 = divmod(left, GRAPH_STEPS)
+    for _ in range(reps2):
+        g.replay()
+    for _ in range(rem2):
+        s.step_with_two_way_coupling(ps)
+    ev[3].record()
+    torch.cuda.synchronize()
+    timed = before + adj_steps
+    el = (ev[0].elapsed_time(ev[1]) + ev[2].elapsed_time(ev[3])) / 1e3
+    stable = bool(s.check_stability())
     done = s.t
-    del s, ps
+    per_step = el / timed
+    fwd_bytes = 77 * cfg.ncell + 268 * pc.count
+    fwd_gbs = fwd_bytes / per_step / 1e9
+    del g, s, ps
     torch.cuda.empty_cache()
     run = OutflowAdjoint(cfg.replace(storage=STORE_F32), adj_steps, ckpt)
     # gradients w.r.t. the band's per-cell porosity (the inlet is more than adj_steps planes
@@ -461,19 +495,48 @@ def scale_row(steps, adj_steps=200, ckpt=20):
     e[2].record()
     torch.cuda.synchronize()
     fwd, bwd = e[0].elapsed_time(e[1]) / 1e3, e[1].elapsed_time(e[2]) / 1e3
+    adj_gbs = 458 * cfg.ncell * adj_steps / bwd / 1e9
     out = {"workload": "%dx%dx%d FP16S + LES(local) + band + %d particles, two-way coupled; adjoint of the outflow "
                        "over the last %d steps (FP32 recompute, checkpoints every %d)"
                        % (cfg.nx, cfg.ny, cfg.nz, pc.count, adj_steps, ckpt),
-           "coupled_steps": done, "coupled_mlups": round(cfg.ncell * n_fwd / el / 1e6, 1),
-           "coupled_ms_per_step": round(el * 1e3 / n_fwd, 4), "stable": stable,
+           "coupled_steps": done, "timed_coupled_steps": timed, "coupled_mlups": round(cfg.ncell / per_step / 1e6, 1),
+           "coupled_ms_per_step": round(per_step * 1e3, 4), "stable": stable,
+           "coupled_roofline": {"algorithmic_bytes_per_step": fwd_bytes, "achieved_gbs": round(fwd_gbs, 1),
+                                "frac": round(fwd_gbs / peak[0], 4), "peak": peak[0], "peak_source": peak[1],
+                                "bytes": "77 B per cell update + 268 B per particle"},
            "adjoint": {"steps": adj_steps, "forward_ms": round(fwd * 1e3, 1), "backward_ms": round(bwd * 1e3, 1),
                        "adjoint_mlups": round(cfg.ncell * adj_steps / bwd / 1e6, 1), "loss": J,
+                       "roofline": {"achieved_gbs": round(adj_gbs, 1), "frac": round(adj_gbs / peak[0], 4),
+                                    "bytes": "458 B per cell update"},
                        "grad_porosity_finite": bool(torch.isfinite(r.grad_porosity).all()),
                        "grad_porosity_nonzero_cells": int((r.grad_porosity != 0).sum().item())},
            "max_memory_gb": round(torch.cuda.max_memory_allocated() / 1e9, 1)}
     del run, nat, eps, r
     torch.cuda.empty_cache()
     return out
+
+
+def run_scale_only(args):
+    """A few coupled steps of the 320x320x384 / 1M-particle case (profiling the coupling kernels)."""
+    import torch
+    from pour_over_coffee_lbm_gb300.params import scale_320x384
+    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    torch.cuda.set_device(0)
+    cfg, pc = scale_320x384()
+    s = GB300LBMSolver(cfg, step_kernel=args.step_kernel)
+    ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
+    ps.seed()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(4):
+        s.step_with_two_way_coupling(ps)
+    start.record()
+    for _ in range(args.steps):
+        s.step_with_two_way_coupling(ps)
+    end.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"scale_only_steps": args.steps, "ms_per_step": round(start.elapsed_time(end) / args.steps, 4),
+                      "stable": bool(s.check_stability())}), flush=True)
 
 
 PRECISION_CASES = {
@@ -491,11 +554,11 @@ def precision_cfg(storage, case):
                          band=kw.get("band", 3.0))
 
 
-def precision_line(storage, steps, peak, case="les_band"):
+def precision_line(storage, steps, peak, case="les_band", step_kernel="registers"):
     import torch
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     cfg = precision_cfg(storage, case)
-    s = GB300LBMSolver(cfg)
+    s = GB300LBMSolver(cfg, step_kernel=step_kernel)
     for _ in range(4):
         s.run(1)
     torch.cuda.synchronize()
@@ -563,8 +626,8 @@ def precision_errors(steps, case="les_band"):
     return res
 
 
-def cpu_baseline(cfg, pc, seconds):
-    """The CPU restatement (oracle, OpenMP on all host cores, particles serial) on the same
+def cpu_baseline_coupled(cfg, pc, seconds):
+    """The CPU restatement (oracle, OpenMP on all host cores, particles serial) on the coupled
     workload, time-bounded: returns MLUPS and the sample it measured."""
     import numpy as np
     import oracle as O
@@ -587,79 +650,121 @@ def cpu_baseline(cfg, pc, seconds):
     return cfg.ncell * steps / el / 1e6, steps, el
 
 
-def run_ours(args):
+def cpu_lattice_steps(cfg, seconds, max_steps):
+    """The CPU restatement's FP32 lattice step (OpenMP on all host cores) on `cfg`, time-bounded:
+    (MLUPS, steps, seconds).  One untimed step first (allocation, page faults)."""
+    import numpy as np
+    import oracle as O
+    flags = O.build_flags(cfg)
+    f = O.init_equilibrium(cfg, flags, np.float32)
+    f, _, _ = O.step(cfg, flags, f)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        f, _, _ = O.step(cfg, flags, f)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= max_steps:
+            break
+    return cfg.ncell * steps / el / 1e6, steps, el
+
+
+HEADLINE = ("256^3 D3Q19 FP32: BGK + Smagorinsky LES (Cs 0.1, local strain) + Guo gravity + 3-cell "
+            "Darcy-Forchheimer filter band (eps 0.6, K 1e-3, C_F 0.55) + half-way bounce-back on the V60 "
+            "cone, inlet disk and drain outlet; no particles")
+REPEATS = 5
+
+
+def headline_cfg():
+    from pour_over_coffee_lbm_gb300.params import STORE_F32
+    return precision_cfg(STORE_F32, "les_band")
+
+
+def step_bytes(solver):
+    """Algorithmic bytes of one plain lattice step: per fluid cell the 19 populations read and
+    written, per cell the 4-byte flag word."""
+    nf = fluid_cells(solver.flags)
+    return nf * 2 * 19 * solver._f.element_size() + solver.n * 4
+
+
+def headline(args, peak, world, local):
+    """The metric's configuration on this GPU: `value` = median over REPEATS timed regions of
+    exactly K steps (graph replays, CUDA events on the launching stream); `e2e` = the same steps
+    through the public solver API with a host->device pour control and a device->host read of the
+    step's FP64 sums every step; `roofline` from the same timing."""
     import torch
-    world, rank, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    torch.cuda.set_device(local)
-    from pour_over_coffee_lbm_gb300 import _lib
-    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
-    lib = _lib.load()
-    peak = peaks()
-    cfg, pc = workload(args.small)
-    solver = GB300LBMSolver(cfg)
-    ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
-    ps.seed()
+    cfg = headline_cfg()
+    s = GB300LBMSolver(cfg, step_kernel=args.step_kernel)
     W = max(3, args.warmup)
-    for _ in range(W):
-        solver.step_with_two_way_coupling(ps)
-    if solver.t % 2:
-        solver.step_with_two_way_coupling(ps)
+    s.run(W + (W % 2))
     torch.cuda.synchronize()
-    graph = solver.capture(GRAPH_STEPS, ps)
+    lib = s.lib
+    graph = s.capture(GRAPH_STEPS)
     graph.replay()
     torch.cuda.synchronize()
     K = args.steps
     reps, rem = divmod(K, GRAPH_STEPS)
-
+    stream = torch.cuda.current_stream()
     clocks = ClockSampler(local)
     clocks.start()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    start = torch.cuda.Event(enable_timing=True)
-    end = torch.cuda.Event(enable_timing=True)
-    start.record(stream)
-    for _ in range(reps):
-        graph.replay()
-    for _ in range(rem):
-        solver.step_with_two_way_coupling(ps)
-    end.record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    elapsed = start.elapsed_time(end) / 1e3
+    times = []
+    lib.pog_launch_count(1)
+    for _ in range(REPEATS):
+        if s.t % 2:
+            s.run(1)  # graphs replay at even time indices
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(reps):
+            graph.replay()
+        if rem:
+            s.run(rem)
+        end.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        times.append(start.elapsed_time(end) / 1e3)
     clk = clocks.stop()
+    eager = int(lib.pog_launch_count(1))
     if world > 1:
-        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        t = torch.tensor(times, device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed = float(t.item())
-    launches = graph.kernels * reps + (rem * (graph.kernels // GRAPH_STEPS))
-    value = world * cfg.ncell * K / elapsed / 1e6
-    diag = solver.get_diagnostics()
+        times = t.tolist()
+    elapsed = statistics.median(times)
+    launches_per_region = graph.kernels // GRAPH_STEPS * GRAPH_STEPS * reps + eager // REPEATS
+    stable = bool(s.check_stability())
+    nbytes = step_bytes(s)
+    per_step = elapsed / K
+    achieved = nbytes / per_step / 1e9
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak[0], "unit": "GB/s",
+            "frac": round(achieved / peak[0], 4), "peak_source": peak[1],
+            "kernel": "rows_step_kernel (row-tiled TMA-staged fused collide-stream) with its bounce-back mailbox "
+                      "passes: one lattice step" if args.step_kernel == "rows" else
+                      "aa_step_kernel (register-staged fused collide-stream): one lattice step",
+            "step_us": round(per_step * 1e6, 2), "algorithmic_bytes_per_step": nbytes,
+            "bytes_per_lup": round(nbytes / s.n, 2), "fluid_cells": fluid_cells(s.flags), "cells": s.n}
 
-    # end to end through the public API: per step H2D pour control, D2H FP64 sums
-    # one pinned slot per step: an async copy never reads a slot the host is rewriting
+    # end to end through the public API: per step an H2D pour control and a D2H of the FP64 sums
     ctl_h = torch.zeros((K, 17), dtype=torch.float32).pin_memory()
     for i in range(K):
         ctl_h[i, 0] = cfg.u_inlet * (1.0 + 0.1 * ((i % 50) / 50.0))  # a slowly varying pour
     ctl_d = torch.zeros(17, dtype=torch.float32, device="cuda")
     ctl_d.copy_(ctl_h[0])
-    solver.set_inlet_control(ctl_d)
+    s.set_inlet_control(ctl_d)
     red_h = torch.zeros((K, 6), dtype=torch.float64).pin_memory()
     for _ in range(2):
-        solver.step_with_two_way_coupling(ps, reduce=True)
+        s.run(1, reduce=True)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for i in range(K):
         ctl_d.copy_(ctl_h[i], non_blocking=True)
-        red = solver.step_with_two_way_coupling(ps, reduce=True)
+        red = s.run(1, reduce=True)
         red_h[i].copy_(red, non_blocking=True)
     torch.cuda.synchronize()
     e2e_el = time.perf_counter() - t0
@@ -668,75 +773,163 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_el = float(t.item())
     e2e_ok = bool(torch.isfinite(red_h[:, :5]).all()) and float(red_h[:, 5].sum()) == 0.0
-    solver.set_inlet_control(None)
+    s.set_inlet_control(None)
+    e2e = {"value": round(world * cfg.ncell * K / e2e_el / 1e6, 1), "unit": "MLUPS",
+           "h2d_bytes_per_step": 17 * 4, "d2h_bytes_per_step": 6 * 8,
+           "api": "GB300LBMSolver.run(1, reduce=True) per step (pog_step through the C ABI)",
+           "results_finite": e2e_ok}
+    out = {"value": world * cfg.ncell * K / elapsed / 1e6, "elapsed": elapsed, "times": times, "K": K, "W": W,
+           "roofline": roof, "e2e": e2e, "clocks": clk, "launches": launches_per_region, "stable": stable,
+           "ncell": cfg.ncell}
+    del graph, s
+    torch.cuda.empty_cache()
+    return out
 
-    roof = kernel_roofline(cfg, pc, max(200, K), peak)
+
+def coupled_line(args, peak):
+    """The 128^3 two-way coupled case (20,000 particles): graph-replayed steps, the public-API
+    coupled step end to end, and the step kernel's roofline."""
+    import torch
+    from pour_over_coffee_lbm_gb300.particles import CoffeeParticleSystem
+    from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
+    cfg, pc = workload(args.small)
+    solver = GB300LBMSolver(cfg, step_kernel=args.step_kernel)
+    ps = CoffeeParticleSystem(pc.count, lattice=cfg, config=pc)
+    ps.seed()
+    for _ in range(max(3, args.warmup)):
+        solver.step_with_two_way_coupling(ps)
+    if solver.t % 2:
+        solver.step_with_two_way_coupling(ps)
+    torch.cuda.synchronize()
+    graph = solver.capture(GRAPH_STEPS, ps)
+    graph.replay()
+    torch.cuda.synchronize()
+    reps = max(1, 200 // GRAPH_STEPS)
+    times = []
+    for _ in range(REPEATS):
+        times.append(time_graph(graph, reps) / (reps * GRAPH_STEPS))
+    per = statistics.median(times)
+    K = reps * GRAPH_STEPS
+    ctl_h = torch.zeros((K, 17), dtype=torch.float32).pin_memory()
+    for i in range(K):
+        ctl_h[i, 0] = cfg.u_inlet * (1.0 + 0.1 * ((i % 50) / 50.0))
+    ctl_d = torch.zeros(17, dtype=torch.float32, device="cuda")
+    ctl_d.copy_(ctl_h[0])
+    solver.set_inlet_control(ctl_d)
+    red_h = torch.zeros((K, 6), dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        solver.step_with_two_way_coupling(ps, reduce=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(K):
+        ctl_d.copy_(ctl_h[i], non_blocking=True)
+        red = solver.step_with_two_way_coupling(ps, reduce=True)
+        red_h[i].copy_(red, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    e2e_ok = bool(torch.isfinite(red_h[:, :5]).all()) and float(red_h[:, 5].sum()) == 0.0
+    solver.set_inlet_control(None)
+    diag = solver.get_diagnostics()
+    out = {"workload": "coupled FP32: %dx%dx%d D3Q19, LES Cs 0.1 (local strain), porous band 3 cells (eps 0.6, "
+                       "K 1e-3, C_F 0.55), %d log-normal particles two-way coupled; a step = coupling pass + "
+                       "lattice step" % (cfg.nx, cfg.ny, cfg.nz, pc.count),
+           "mlups": round(cfg.ncell / per / 1e6, 1), "ms_per_step": round(per * 1e3, 4),
+           "repeats_ms_per_step": [round(t * 1e3, 4) for t in times],
+           "kernels_per_step": graph.kernels // GRAPH_STEPS,
+           "e2e": {"value": round(cfg.ncell * K / e2e_el / 1e6, 1), "unit": "MLUPS", "h2d_bytes_per_step": 68,
+                   "d2h_bytes_per_step": 48, "results_finite": e2e_ok,
+                   "api": "GB300LBMSolver.step_with_two_way_coupling(reduce=True) per step"},
+           "stable": diag["stable"],
+           "l2": "distributions %.0f MB > 129 MB L2 (no flush)" % (19 * 4 * cfg.ncell / 1e6)}
+    del graph, solver, ps
+    torch.cuda.empty_cache()
+    out["roofline"] = kernel_roofline(cfg, pc, 200, peak, args.step_kernel)
     traffic_path = os.path.join(ROOT, "profiles", "aa_step_traffic.json")
-    roof["traffic"] = None
     if os.path.exists(traffic_path):
         with open(traffic_path) as fh:
             tr = json.load(fh)
-        key = "%dx%dx%d" % (cfg.nx, cfg.ny, cfg.nz)
+        key = "coupled %dx%dx%d" % (cfg.nx, cfg.ny, cfg.nz)
         if key in tr:
-            roof["traffic"] = tr[key]["bytes_per_launch"]
-            roof["traffic_source"] = tr[key].get("source")
+            out["roofline"]["traffic"] = tr[key]["bytes_per_launch"]
+            out["roofline"]["traffic_source"] = tr[key].get("source")
+    if not args.no_cpu:
+        mlups, steps, el = cpu_baseline_coupled(cfg, pc, min(args.cpu_seconds, 10.0))
+        out["cpu_baseline"] = {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "%d coupled steps of this workload (%.1f s), CPU restatement (OpenMP "
+                                         "lattice, serial particles)" % (steps, el)}
+    return out
 
-    extra = None
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from pour_over_coffee_lbm_gb300 import _lib
+    _lib.load()
+    peak = peaks()
+    h = headline(args, peak, world, local)
+    traffic_path = os.path.join(ROOT, "profiles", "aa_step_traffic.json")
+    h["roofline"]["traffic"] = None
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as fh:
+            tr = json.load(fh)
+        key = "les_band 256x256x256 fp32 %s" % args.step_kernel
+        if key in tr:
+            h["roofline"]["traffic"] = tr[key]["bytes_per_step"]
+            h["roofline"]["traffic_source"] = tr[key].get("source")
+
+    extra = coupled = rows = diff = scale = None
     if not args.no_extra and not args.small and rank == 0:
         from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
-        del graph
-        torch.cuda.empty_cache()
         extra = {}
         for case, label in (("les_band", "256^3 D3Q19 + LES(local) + porous band, no particles"),
                             ("plain", "256^3 D3Q19, gravity + inlet/outlet + cone walls (no LES, no band)")):
-            p32 = precision_line(STORE_F32, 200, peak, case)
-            p16 = precision_line(STORE_F16S, 200, peak, case)
-            pb16 = precision_line(STORE_BF16S, 200, peak, case)
+            lines = {}
+            for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
+                lines[name] = {k: precision_line(st, 200, peak, case, k) for k in ("rows", "registers")}
+            best = {n: max(v.values(), key=lambda d: d["mlups"]) for n, v in lines.items()}
             errs = precision_errors(args.error_steps, case) if args.error_steps > 0 else None
-            extra[case] = {"workload": label, "fp32": p32, "fp16s": p16, "bf16s": pb16, "error_vs_fp64": errs,
-                           "fp16s_vs_fp32_mlups": round(p16["mlups"] / p32["mlups"], 3),
-                           "bf16s_vs_fp32_mlups": round(pb16["mlups"] / p32["mlups"], 3)}
-
-    rows = diff = scale = None
-    if not args.no_extra and not args.small and rank == 0:
-        rows = plugin_rows(cfg, pc, 200, peak)
+            extra[case] = {"workload": label, "lines": lines, "error_vs_fp64": errs,
+                           "fp16s_vs_fp32_mlups": round(best["fp16s"]["mlups"] / best["fp32"]["mlups"], 3),
+                           "bf16s_vs_fp32_mlups": round(best["bf16s"]["mlups"] / best["fp32"]["mlups"], 3)}
+        coupled = coupled_line(args, peak)
+        rows = plugin_rows(*workload(False), 200, peak)
         diff = differentiation_rows(peak)
         if args.scale_steps > 0:
-            scale = scale_row(args.scale_steps)
+            scale = scale_row(args.scale_steps, peak, step_kernel=args.step_kernel)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        mlups, steps, el = cpu_baseline(cfg, pc, args.cpu_seconds)
+        mlups, steps, el = cpu_lattice_steps(headline_cfg(), args.cpu_seconds, 200)
         cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
-               "sample": "%d coupled steps of the same %dx%dx%d + %d-particle workload (%.1f s), "
-                         "CPU restatement (OpenMP lattice, serial particles)"
-                         % (steps, cfg.nx, cfg.ny, cfg.nz, pc.count, el)}
+               "sample": "%d FP32 lattice steps of the same 256^3 LES + porous-band workload (%.1f s), the CPU "
+                         "restatement of the reference path (OpenMP on all host cores)" % (steps, el)}
 
     if rank == 0:
         line = {
             "metric": "D3Q19 MLUPS & % HBM roofline; FP16-store vs FP32 MLUPS at <=1e-3 rel err",
-            "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
-            "ms_per_step": round(elapsed * 1e3 / K, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded V60 geometry and particles)",
-            "config": {"workload": "coupled FP32: %dx%dx%d D3Q19, LES Cs 0.1 (local strain), porous band 3 cells "
-                                   "(eps 0.6, K 1e-3, C_F 0.55), %d log-normal particles two-way coupled"
-                                   % (cfg.nx, cfg.ny, cfg.nz, pc.count),
-                       "cells": cfg.ncell, "particles": pc.count, "graph_steps": GRAPH_STEPS,
-                       "l2": "distributions %.0f MB > 129 MB L2 (no flush)" % (19 * 4 * cfg.ncell / 1e6),
+            "value": round(h["value"], 1), "unit": "MLUPS", "n_gpus": world, "steps": h["K"], "warmup": h["W"],
+            "ms_per_step": round(h["elapsed"] * 1e3 / h["K"], 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded V60 geometry)",
+            "config": {"workload": HEADLINE, "cells": h["ncell"], "step_kernel": args.step_kernel,
+                       "graph_steps": GRAPH_STEPS, "repeats": REPEATS,
+                       "repeat_ms_per_step": [round(t * 1e3 / h["K"], 4) for t in h["times"]],
+                       "l2": "distributions %.2f GB > 129 MB L2 (no flush needed)" % (19 * 4 * h["ncell"] / 1e9),
                        "parallelism": "replicas x%d (one independent lattice per GPU)" % world},
-            "e2e": {"value": round(world * cfg.ncell * K / e2e_el / 1e6, 1), "unit": "MLUPS",
-                    "h2d_bytes_per_step": 17 * 4, "d2h_bytes_per_step": 6 * 8,
-                    "api": "GB300LBMSolver.step_with_two_way_coupling(reduce=True) per step",
-                    "results_finite": e2e_ok},
-            "gpu_launches": int(launches),
-            "roofline": roof,
+            "e2e": h["e2e"],
+            "gpu_launches": int(h["launches"]),
+            "roofline": h["roofline"],
             "cpu_baseline": cpu,
-            "clocks": clk,
+            "clocks": h["clocks"],
+            "stable": h["stable"],
             "precision_256": extra,
+            "coupled_128": coupled,
             "plugin_rows": rows,
             "differentiation_96": diff,
             "scale_320x320x384": scale,
-            "diagnostics": {"mass": diag["mass"], "max_velocity": diag["max_velocity"], "stable": diag["stable"]},
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -744,51 +937,39 @@ def run_ours(args):
 
 
 def run_reference(args):
+    """The reference arm: the reference's path on the host cores.  The reference is Python +
+    Taichi and cannot be installed here, so this times its CPU restatement (the oracle, OpenMP on
+    all host cores) on the same 256^3 workload, each step a full lattice step, bounded so the run
+    ends within about two minutes."""
     world, rank, local = dist_env()
     if rank != 0:
         return
-    cfg, pc = workload(args.small)
-    # each step of this arm is one coupled step of the CPU restatement; the run is bounded to
-    # about two minutes by timing at most the steps that fit (reported in `sample`)
     import numpy as np
     import oracle as O
-    from pour_over_coffee_lbm_gb300.params import seed_particles
+    cfg = headline_cfg()
     flags = O.build_flags(cfg)
     f = O.init_equilibrium(cfg, flags, np.float32)
-    pos, vel, d, act = seed_particles(cfg, pc)
-    drag = np.zeros_like(pos)
-    _, _, u = O.step(cfg, flags, f)
-
-    def one():
-        nonlocal pos, vel, drag, act, f, u
-        pos, vel, drag, act, fix, _ = O.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
-        pdrag = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(4, cfg.nz, cfg.ny, cfg.nx)
-        f, _, u = O.step(cfg, flags, f, pdrag=pdrag)
-
     W = max(3, args.warmup)
     t0 = time.perf_counter()
-    one()
+    f, _, _ = O.step(cfg, flags, f)
     per = time.perf_counter() - t0
-    wsteps = min(W, max(1, int(20.0 / per)))
-    for _ in range(wsteps - 1):
-        one()
+    for _ in range(min(W, max(1, int(20.0 / per))) - 1):
+        f, _, _ = O.step(cfg, flags, f)
     K = args.steps
     k_run = min(K, max(3, int(120.0 / per)))
     t0 = time.perf_counter()
     for _ in range(k_run):
-        one()
+        f, _, _ = O.step(cfg, flags, f)
     el = time.perf_counter() - t0
     mlups = cfg.ncell * k_run / el / 1e6
     line = {"impl": "reference",
             "metric": "D3Q19 MLUPS & % HBM roofline; FP16-store vs FP32 MLUPS at <=1e-3 rel err",
             "value": round(mlups, 3), "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": round(el * 1e3 / k_run, 3), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded V60 geometry and particles)",
-            "config": {"workload": "coupled FP32: %dx%dx%d D3Q19, LES Cs 0.1 (local strain), porous band 3 cells "
-                                   "(eps 0.6, K 1e-3, C_F 0.55), %d log-normal particles two-way coupled"
-                                   % (cfg.nx, cfg.ny, cfg.nz, pc.count)},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded V60 geometry)",
+            "config": {"workload": HEADLINE, "cells": cfg.ncell},
             "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
-                             "sample": "%d of %d requested coupled steps timed (%.1f s); the reference is "
+                             "sample": "%d of %d requested lattice steps timed (%.1f s); the reference is "
                                        "Python+Taichi (not installable here), this is its CPU restatement"
                                        % (k_run, K, el)},
             "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -800,14 +981,16 @@ def run_precision_only(args):
     from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
     torch.cuda.set_device(0)
     st = {"fp32": STORE_F32, "fp16s": STORE_F16S, "bf16s": STORE_BF16S}[args.precision_only]
-    out = precision_line(st, max(GRAPH_STEPS, args.steps), peaks(), args.precision_case)
-    print(json.dumps({"precision_only": args.precision_only, **out}), flush=True)
+    out = precision_line(st, max(GRAPH_STEPS, args.steps), peaks(), args.precision_case, args.step_kernel)
+    print(json.dumps({"precision_only": args.precision_only, "step_kernel": args.step_kernel, **out}), flush=True)
 
 
 def main():
     args = parse()
     if args.precision_only:
         run_precision_only(args)
+    elif args.scale_only:
+        run_scale_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
