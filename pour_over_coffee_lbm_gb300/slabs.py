@@ -242,3 +242,112 @@ class RankHalo:
         self._trade(above, f[UP, self.top + 1], below, buf)
         if below is not None:
             f[UP, 1] = torch.where(self.m_up, buf, f[UP, 1])
+
+
+def owner_plane(z: torch.Tensor, nz: int) -> torch.Tensor:
+    """The cell plane a particle at height z gathers from: int(clamp(z, 0, nz - 2))
+    (coffee_particles.py:1162-1164), the plane that decides which slab owns it."""
+    return torch.clamp(z, 0.0, float(nz - 2)).to(torch.int64)
+
+
+class RankParticles:
+    """Particles owned by z-slab, one slab per rank, coupled to a RankHalo lattice.
+
+    A particle belongs to the rank whose planes [z0, z1) contain its cell plane
+    k = int(clamp(z, 0, nz - 2)); its trilinear corners are planes k and k + 1, so the coupling
+    pass of the rank reads planes z0 .. z1 and writes its deposit there.  Around each pass:
+
+      exchange_u      before it: the velocity of the first owned plane goes down into the lower
+                      neighbour's top ghost plane (particles in plane z1 - 1 gather from z1);
+      reduce_deposit  after it: the deposit in the top ghost plane goes up and is added to the
+                      upper neighbour's first owned plane (the spread's reduce-add);
+      migrate         particles whose cell plane left [z0, z1) move to the neighbour that owns it
+                      (one plane per step at most: the lattice velocity is far below one cell per
+                      step).
+
+    Slab tensors have the RankHalo layout [..., z1 - z0 + 2, ny, nx] (ghost below | owned | ghost
+    above).  With the fixed-point (int64) deposit of deterministic mode the reduce-add is exact,
+    so a decomposed coupled run repeats the undivided one bit for bit."""
+
+    FIELDS = ("pos", "vel", "diam", "drag_old", "active", "ident")
+
+    def __init__(self, rank: int, world: int, z0: int, z1: int, nz: int):
+        import torch.distributed as dist
+        self.dist = dist
+        self.rank, self.world = rank, world
+        self.z0, self.z1, self.nz = z0, z1, nz
+        self.below = rank - 1 if rank > 0 else None
+        self.above = rank + 1 if rank < world - 1 else None
+
+    def _trade(self, send_to, send_buf, recv_from, recv_buf):
+        ops = []
+        if send_to is not None:
+            ops.append(self.dist.P2POp(self.dist.isend, send_buf.contiguous(), send_to))
+        if recv_from is not None:
+            ops.append(self.dist.P2POp(self.dist.irecv, recv_buf, recv_from))
+        if ops:
+            for r in self.dist.batch_isend_irecv(ops):
+                r.wait()
+
+    def exchange_u(self, u: torch.Tensor) -> None:
+        """u [3, nzs + 2, ny, nx]: fill the top ghost plane from the upper neighbour."""
+        top = u.shape[1] - 1
+        buf = torch.empty_like(u[:, 0])
+        self._trade(self.below, u[:, 1], self.above, buf)
+        if self.above is not None:
+            u[:, top] = buf
+
+    def reduce_deposit(self, dep: torch.Tensor) -> None:
+        """dep [4, nzs + 2, ny, nx]: send the top ghost plane up, add the lower neighbour's into
+        the first owned plane, and clear the ghost planes."""
+        top = dep.shape[1] - 1
+        buf = torch.empty_like(dep[:, 0])
+        self._trade(self.above, dep[:, top], self.below, buf)
+        if self.below is not None:
+            dep[:, 1] += buf
+        dep[:, 0] = 0
+        dep[:, top] = 0
+
+    def migrate(self, parts: dict) -> dict:
+        """parts: the FIELDS as tensors over this rank's particles (pos/vel/drag_old [3, m], the
+        rest [m]).  Returns the particles this rank owns after the move, its own first (in their
+        order), then those received from below, then from above."""
+        k = owner_plane(parts["pos"][2], self.nz)
+        down = k < self.z0
+        up = k >= self.z1
+        keep = ~(down | up)
+        if (down.any() and self.below is None) or (up.any() and self.above is None):
+            raise RuntimeError("a particle left the domain's slabs")
+
+        def pick(mask):
+            return {f: (v[:, mask] if v.dim() == 2 else v[mask]) for f, v in parts.items()}
+
+        dev = parts["pos"].device
+
+        def exchange(to, mask, frm):
+            # counts first, then one message per field
+            n_out = torch.tensor([int(mask.sum())], dtype=torch.int64, device=dev)
+            n_in = torch.zeros(1, dtype=torch.int64, device=dev)
+            self._trade(to, n_out, frm, n_in)
+            out = pick(mask)
+            got = {}
+            for f, v in parts.items():
+                shape = (v.shape[0], int(n_in)) if v.dim() == 2 else (int(n_in),)
+                buf = torch.empty(shape, dtype=v.dtype, device=dev)
+                self._trade(to, out[f], frm, buf)
+                got[f] = buf
+            return got
+
+        # downward moves first (every rank sends down / receives from above), then upward
+        from_above = exchange(self.below, down, self.above)
+        from_below = exchange(self.above, up, self.below)
+        mine = pick(keep)
+        res = {}
+        for f in parts:
+            parts_f = [mine[f]]
+            if self.below is not None:
+                parts_f.append(from_below[f])
+            if self.above is not None:
+                parts_f.append(from_above[f])
+            res[f] = torch.cat(parts_f, dim=-1)
+        return res

@@ -186,3 +186,118 @@ def test_rank_halo_with_the_oracle_aa_step(tmp_path, world):
         got[:, z0:z1] = _natural(fs, slab_flags(flags, z0, z1), ORC_STEPS)[:, 1:-1]
     assert np.array_equal(got[:, live], ref[:, live])
     assert np.abs(ref[:, live] - f0[:, live]).max() > 1e-4  # the state did evolve
+
+
+# ---- slab-owned particles (RankParticles) with the oracle's coupling pass and AA step --------------
+P_STEPS = 10
+
+
+def _coupled_slab_case():
+    from pour_over_coffee_lbm_gb300.params import LES_LOCAL, LatticeConfig, ParticleConfig
+    cfg = LatticeConfig(nx=20, ny=18, nz=28, band_thickness=2.0, les_mode=LES_LOCAL, u_inlet=-0.05, cs_smag=0.3)
+    pc = ParticleConfig(count=600, deterministic=True, density_ratio=1.5)
+    rng = np.random.default_rng(31)
+    n = pc.count
+    cx, cy = cfg.axis
+    # particles around the interfaces z = 9 and z = 18 of three slabs, moving up or down across them
+    zc = np.where(rng.uniform(size=n) < 0.5, 9.0, 18.0)
+    z = zc + rng.uniform(-0.3, 0.3, n)
+    r = 0.5 * (z - cfg.cone_apex_z) * np.tan(np.radians(cfg.cone_half_angle_deg)) * np.sqrt(rng.uniform(size=n))
+    a = rng.uniform(0, 2 * np.pi, n)
+    pos = np.stack([cx + r * np.cos(a), cy + r * np.sin(a), z]).astype(np.float32)
+    vel = np.zeros((3, n), np.float32)
+    vel[2] = rng.choice([-0.15, 0.15], n).astype(np.float32)
+    d = np.exp(rng.normal(np.log(0.6), 0.3, n)).astype(np.float32)
+    act = np.ones(n, np.int32)
+    return cfg, pc, pos, vel, d, act
+
+
+def _rank_particles(rank, world, port, outdir):
+    import oracle
+    from pour_over_coffee_lbm_gb300.slabs import RankParticles, owner_plane
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    cfg, pc, pos, vel, d, act = _coupled_slab_case()
+    nz, ny, nx = cfg.nz, cfg.ny, cfg.nx
+    flags = oracle.build_flags(cfg)
+    z0, z1 = slab_bounds(nz, world)[rank]
+    fl = slab_flags(flags, z0, z1)
+    nzs = z1 - z0 + 2
+    scfg = cfg.replace(nz=nzs)
+    f = oracle.init_equilibrium(cfg, flags, np.float32)
+    fs = np.zeros((19, nzs, ny, nx), np.float32)
+    lo, hi = max(z0 - 1, 0), min(z1 + 1, nz)
+    fs[:, lo - (z0 - 1): hi - (z0 - 1)] = f[:, lo:hi]
+    ft = torch.from_numpy(fs)
+    halo = RankHalo(fl, rank, world)
+    rp = RankParticles(rank, world, z0, z1, nz)
+    k = owner_plane(torch.from_numpy(pos[2]), nz)
+    mine = ((k >= z0) & (k < z1)).numpy()
+    parts = {"pos": torch.from_numpy(pos[:, mine].copy()), "vel": torch.from_numpy(vel[:, mine].copy()),
+             "diam": torch.from_numpy(d[mine].copy()), "drag_old": torch.zeros((3, int(mine.sum())), dtype=torch.float32),
+             "active": torch.from_numpy(act[mine].copy()), "ident": torch.arange(pc.count)[torch.from_numpy(mine)]}
+    u = torch.zeros((3, nzs, ny, nx), dtype=torch.float32)
+    moved = 0
+    for t in range(P_STEPS):
+        rp.exchange_u(u)
+        ug = np.zeros((3, nz, ny, nx), np.float32)  # this slab's planes z0 - 1 .. z1 of the global u
+        ug[:, lo:hi] = u.numpy()[:, lo - (z0 - 1): hi - (z0 - 1)]
+        ppos, pvel, pdrag_old, pact, fix, _ = oracle.particles_couple(
+            cfg, pc, parts["pos"].numpy(), parts["vel"].numpy(), parts["diam"].numpy(), parts["drag_old"].numpy(),
+            parts["active"].numpy(), ug)
+        fix = fix.reshape(4, nz, ny, nx)
+        assert not fix[:, :z0].any() and not fix[:, z1 + 1:].any()  # corners stay within z0 .. z1
+        dep = torch.zeros((4, nzs, ny, nx), dtype=torch.int64)
+        dep[:, lo - (z0 - 1): hi - (z0 - 1)] = torch.from_numpy(fix[:, lo:hi])
+        rp.reduce_deposit(dep)
+        pdrag = (dep.double() / 2.0 ** 32).float().numpy()
+        parts.update(pos=torch.from_numpy(ppos), vel=torch.from_numpy(pvel), drag_old=torch.from_numpy(pdrag_old),
+                     active=torch.from_numpy(pact))
+        before = parts["ident"].clone()
+        parts = rp.migrate(parts)
+        moved += int((~torch.isin(parts["ident"], before)).sum())
+        if t % 2:
+            halo.exchange_in(ft)
+        _, un = oracle.step_aa(scfg, fl, fs, t, pdrag=pdrag, macro=True)
+        if t % 2:
+            halo.exchange_out(ft)
+        u = torch.from_numpy(un)
+    if P_STEPS % 2:
+        halo.exchange_in(ft)
+    np.savez(os.path.join(outdir, "pslab%d.npz" % rank), f=fs, moved=moved,
+             **{k: v.numpy() for k, v in parts.items()})
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_slab_owned_particles_match_undivided(tmp_path):
+    """Three gloo ranks, particles owned by slab: the u ghost plane, the deposit's reduce-add and
+    the migration across the interfaces reproduce the undivided coupled run bit for bit."""
+    import oracle
+    world = 3
+    cfg, pc, pos, vel, d, act = _coupled_slab_case()
+    flags = oracle.build_flags(cfg)
+    f = oracle.init_equilibrium(cfg, flags, np.float32)
+    u = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), np.float32)
+    drag = np.zeros_like(pos)
+    for t in range(P_STEPS):
+        pos, vel, drag, act, fix, _ = oracle.particles_couple(cfg, pc, pos, vel, d, drag, act, u)
+        pdrag = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(4, cfg.nz, cfg.ny, cfg.nx)
+        _, u = oracle.step_aa(cfg, flags, f, t, pdrag=pdrag, macro=True)
+    ref = _natural(f, flags, P_STEPS)
+    mp.start_processes(_rank_particles, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    got = np.zeros_like(f)
+    gpos = np.full_like(pos, np.nan)
+    seen = np.zeros(pc.count, int)
+    moved = 0
+    for r, (z0, z1) in enumerate(slab_bounds(cfg.nz, world)):
+        z = np.load(tmp_path / ("pslab%d.npz" % r))
+        got[:, z0:z1] = _natural(z["f"], slab_flags(flags, z0, z1), P_STEPS)[:, 1:-1]
+        gpos[:, z["ident"]] = z["pos"]
+        seen[z["ident"]] += 1
+        moved += int(z["moved"])
+    live = np.zeros(flags.shape, bool)
+    live[1:-1, 1:-1, 1:-1] = (flags[1:-1, 1:-1, 1:-1] & 1) == 0
+    assert np.all(seen == 1)  # every particle owned by exactly one rank
+    assert moved > 20  # particles did cross the interfaces
+    assert np.array_equal(gpos, pos)
+    assert np.array_equal(got[:, live], ref[:, live])
