@@ -470,14 +470,24 @@ int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* 
  *   pdrag     [4][ncell] the particle drag deposit (Kp, Kv) the forward step read, or NULL: a
  *             fixed input, its force Kv - Kp u differentiated through u (the coupled step of
  *             legacy/lbm_solver.py:1485-1509 with the particles' deposit recorded per step)
+ *   LES stencil mode (les_turbulence.py:318-380: step t's nu_sgs reads the velocity u_{t-1} that
+ *   step t-1 output, so dJ/du crosses steps):
+ *   u_prev     [3][ncell] float, the velocity the forward step's stencil read (required)
+ *   dJ_du      [3][ncell] (storage type) dJ/du_t of the velocity this step outputs, or NULL (0)
+ *   dJ_du_prev [3][ncell] receives dJ/du_{t-1} (overwritten; required, != dJ_du)
+ *   scratch    pog_adjoint_scratch_bytes(p) bytes of device memory (required)
+ *   In the other LES modes these four are ignored (pass NULL).
  *   The loss is J = sum_t flux_t with flux_t = POG_RED_OUTFLOW of step t, so each outlet
  *   cell adds dJ/df_i = -c_iz.  Parameter gradients are accumulated in FP64:
  *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
- *   Supported: les_mode OFF/LOCAL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL,
+ *   Supported: les_mode OFF/LOCAL/STENCIL, drag SEMI_IMPLICIT, forcing GUO, clamp_tau 0, force NULL,
  *   pour_control, filter_blockage and phase NULL (POG_E_ARG otherwise). */
 int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next, void* lam_t,
                      const uint32_t* flags, const float* porosity, const float* pdrag,
+                     const float* u_prev, const void* dJ_du, void* dJ_du_prev, void* scratch,
                      double* grad_porosity, double* grad_inlet, void* stream);
+/* Scratch pog_adjoint_step needs in LES stencil mode (10 values per cell), 0 otherwise. */
+size_t pog_adjoint_scratch_bytes(const pog_params* p);
 
 /* The outflow flux of a natural-layout state f_nat (F32 or F64 storage), flux = -sum over outlet
  * cells of sum_q c_qz f_q -- the POG_RED_OUTFLOW contribution of the step that starts from f_nat --

@@ -371,9 +371,12 @@ def particles_couple(cfg, pcfg, pos, vel, diam, drag_old, active, u, force_fix=N
     return pos, vel, drag_old, active, force_fix, u_at
 
 
-def adjoint_step(cfg, flags, f_t, lam_next, eps=None, grad_eps=None, grad_inlet=None, pdrag=None):
+def adjoint_step(cfg, flags, f_t, lam_next, eps=None, grad_eps=None, grad_inlet=None, pdrag=None,
+                 u_prev=None, mu_in=None, mu_out=None):
     """Adjoint of one FP64 push step by forward-mode dual numbers; pdrag: the step's particle drag
-    deposit [4][n] (float32), held fixed."""
+    deposit [4][n] (float32), held fixed.  LES stencil mode: u_prev [3][n] the velocity the step's
+    nu_sgs reads, mu_in dJ/du of the velocity the step outputs, mu_out (float64 [3][n], added to)
+    receives dJ/du_prev."""
     lib = load()
     _, pp = _params(cfg)
     lam_t = np.zeros_like(lam_next)
@@ -381,9 +384,17 @@ def adjoint_step(cfg, flags, f_t, lam_next, eps=None, grad_eps=None, grad_inlet=
         eps = np.ascontiguousarray(eps, np.float32)
     if pdrag is not None:
         pdrag = np.ascontiguousarray(pdrag, np.float32)
-    lib.orc_adjoint_step_f64(pp, _p(flags), _p(np.ascontiguousarray(f_t, np.float64)),
-                             _p(np.ascontiguousarray(lam_next, np.float64)), _p(lam_t), _p(eps), _p(pdrag),
-                             _p(grad_eps), _p(grad_inlet))
+    if u_prev is not None:
+        u_prev = np.ascontiguousarray(u_prev, np.float64)
+    if mu_in is not None:
+        mu_in = np.ascontiguousarray(mu_in, np.float64)
+    if mu_out is not None:
+        assert mu_out.dtype == np.float64 and mu_out.flags.c_contiguous
+    rc = lib.orc_adjoint_step_f64(pp, _p(flags), _p(np.ascontiguousarray(f_t, np.float64)),
+                                  _p(np.ascontiguousarray(lam_next, np.float64)), _p(lam_t), _p(eps), _p(pdrag),
+                                  _p(u_prev), _p(mu_in), _p(mu_out), _p(grad_eps), _p(grad_inlet))
+    if rc != 0:
+        raise ValueError("the stencil-mode adjoint needs u_prev")
     return lam_t
 
 
@@ -399,13 +410,21 @@ def outflow_gradient(cfg, nsteps, flags=None, eps=None):
     if flags is None:
         flags = build_flags(cfg)
     f = init_equilibrium(cfg, flags, np.float64)
-    states = []
+    stencil = cfg.les_mode == 1
+    u = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), np.float64)
+    states, uprevs = [], []
     for _ in range(nsteps):
         states.append(f)
-        f, _, _ = step(cfg, flags, f, eps=eps)
+        uprevs.append(u)
+        f, _, u = step(cfg, flags, f, eps=eps, u_prev=u if stencil else None)
     lam = np.zeros_like(f)
+    mu = np.zeros((3, cfg.nz, cfg.ny, cfg.nx), np.float64)
     ge = np.zeros((cfg.nz, cfg.ny, cfg.nx), np.float64) if eps is not None else None
     gi = np.zeros(16, np.float64)
     for t in reversed(range(nsteps)):
-        lam = adjoint_step(cfg, flags, states[t], lam, eps=eps, grad_eps=ge, grad_inlet=gi)
+        mu_out = np.zeros_like(mu) if stencil else None
+        lam = adjoint_step(cfg, flags, states[t], lam, eps=eps, grad_eps=ge, grad_inlet=gi,
+                           u_prev=uprevs[t] if stencil else None, mu_in=mu if stencil else None, mu_out=mu_out)
+        if stencil:
+            mu = mu_out
     return ge, gi

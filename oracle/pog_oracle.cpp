@@ -166,24 +166,16 @@ void porous_coeffs(const pog_params* p, T eps, T& K, T& CF) {
 
 // LES nu_sgs from central differences of a stored velocity field
 // (les_turbulence.py:318-380).  u is [3][n].  Returns 0 where the reference does.
+// nu_sgs from the velocities of the six neighbours, un[m][a]: m = (i+1, i-1, j+1, j-1, k+1, k-1),
+// a = (x, y, z) component.
 template <typename T>
-T les_nu_stencil(const pog_params* p, const Geo& g, const uint32_t* flags, const T* u, int i,
-                 int j, int k) {
-  if (i < 1 || j < 1 || k < 1 || i > g.nx - 2 || j > g.ny - 2 || k > g.nz - 2) return 0;
-  long long c = g.idx(i, j, k);
-  if (flags[c] & POG_CELL_POROUS) return 0;  // filter zone: LES mask 0 (filter_paper.py:199)
-  const T* ux = u;
-  const T* uy = u + g.n;
-  const T* uz = u + 2 * g.n;
-  long long ip = g.idx(i + 1, j, k), im = g.idx(i - 1, j, k);
-  long long jp = g.idx(i, j + 1, k), jm = g.idx(i, j - 1, k);
-  long long kp = g.idx(i, j, k + 1), km = g.idx(i, j, k - 1);
-  T dudx = (ux[ip] - ux[im]) * (T)0.5, dudy = (ux[jp] - ux[jm]) * (T)0.5,
-    dudz = (ux[kp] - ux[km]) * (T)0.5;
-  T dvdx = (uy[ip] - uy[im]) * (T)0.5, dvdy = (uy[jp] - uy[jm]) * (T)0.5,
-    dvdz = (uy[kp] - uy[km]) * (T)0.5;
-  T dwdx = (uz[ip] - uz[im]) * (T)0.5, dwdy = (uz[jp] - uz[jm]) * (T)0.5,
-    dwdz = (uz[kp] - uz[km]) * (T)0.5;
+T les_nu_from_neighbours(const pog_params* p, const T un[6][3]) {
+  T dudx = (un[0][0] - un[1][0]) * (T)0.5, dudy = (un[2][0] - un[3][0]) * (T)0.5,
+    dudz = (un[4][0] - un[5][0]) * (T)0.5;
+  T dvdx = (un[0][1] - un[1][1]) * (T)0.5, dvdy = (un[2][1] - un[3][1]) * (T)0.5,
+    dvdz = (un[4][1] - un[5][1]) * (T)0.5;
+  T dwdx = (un[0][2] - un[1][2]) * (T)0.5, dwdy = (un[2][2] - un[3][2]) * (T)0.5,
+    dwdz = (un[4][2] - un[5][2]) * (T)0.5;
   T S11 = dudx, S22 = dvdy, S33 = dwdz;
   T S12 = (T)0.5 * (dudy + dvdx), S13 = (T)0.5 * (dudz + dwdx), S23 = (T)0.5 * (dvdz + dwdy);
   T smag = sqrt((T)2 * (S11 * S11 + S22 * S22 + S33 * S33 +
@@ -192,6 +184,36 @@ T les_nu_stencil(const pog_params* p, const Geo& g, const uint32_t* flags, const
   T cs = (T)p->cs_smag;
   T nu = cs * cs * smag;
   return std::min(nu, (T)p->les_nu_max);
+}
+
+// Cell offsets of the six stencil neighbours, in les_nu_from_neighbours' order.
+inline void stencil_neighbours(const Geo& g, int i, int j, int k, long long nb[6]) {
+  nb[0] = g.idx(i + 1, j, k);
+  nb[1] = g.idx(i - 1, j, k);
+  nb[2] = g.idx(i, j + 1, k);
+  nb[3] = g.idx(i, j - 1, k);
+  nb[4] = g.idx(i, j, k + 1);
+  nb[5] = g.idx(i, j, k - 1);
+}
+
+// Whether cell (i, j, k) takes a stencil nu at all (interior, outside the filter zone's LES mask).
+inline bool les_stencil_cell(const Geo& g, const uint32_t* flags, int i, int j, int k) {
+  if (i < 1 || j < 1 || k < 1 || i > g.nx - 2 || j > g.ny - 2 || k > g.nz - 2) return false;
+  return !(flags[g.idx(i, j, k)] & POG_CELL_POROUS);  // filter zone: LES mask 0 (filter_paper.py:199)
+}
+
+// LES nu_sgs from central differences of a stored velocity field
+// (les_turbulence.py:318-380).  u is [3][n].  Returns 0 where the reference does.
+template <typename T>
+T les_nu_stencil(const pog_params* p, const Geo& g, const uint32_t* flags, const T* u, int i,
+                 int j, int k) {
+  if (!les_stencil_cell(g, flags, i, j, k)) return 0;
+  long long nb[6];
+  stencil_neighbours(g, i, j, k, nb);
+  T un[6][3];
+  for (int m = 0; m < 6; ++m)
+    for (int a = 0; a < 3; ++a) un[m][a] = u[a * g.n + nb[m]];
+  return les_nu_from_neighbours<T>(p, un);
 }
 
 // Per-cell collision (legacy/lbm_solver.py:488-535 moments, :537-579 BGK, :594-607/688-764
@@ -1017,7 +1039,7 @@ float orc_round_storage(int storage, float v, int q, float rho0) {
 // lam* pulled through the transpose of push streaming.  This is automatic differentiation of
 // the restatement, independent of the hand-derived CUDA adjoint it checks.
 namespace {
-const int ND = 19 + 1 + POG_INLET_NCOEF;  // f_q, eps, a_k
+const int ND = 19 + 1 + POG_INLET_NCOEF + 18;  // f_q, eps, a_k, the stencil neighbours' u
 struct Dual {
   double v;
   double d[ND];
@@ -1072,9 +1094,16 @@ inline Dual sqrt(const Dual& a) {
 
 // Pd (nullable): the step's particle drag deposit [4][n] (Kp, Kv), a fixed input (constants in
 // the dual numbers), as the CUDA adjoint takes it.
+// LES stencil mode: u_prev [3][n] is the velocity the step's nu_sgs reads (the previous step's
+// output), mu_in [3][n] (nullable) dJ/du of the velocity this step outputs (read by the next
+// step's stencil), mu_out [3][n] receives (+=) dJ/du_prev; the six neighbours' velocities are
+// seeded as dual directions 36..53.
 extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint32_t* flags, const double* ft,
                                     const double* lam_next, double* lam_t, const float* eps,
-                                    const float* Pd, double* grad_eps, double* grad_inlet) {
+                                    const float* Pd, const double* u_prev, const double* mu_in,
+                                    double* mu_out, double* grad_eps, double* grad_inlet) {
+  const bool stencil = p->les_mode == POG_LES_STENCIL;
+  if (stencil && !u_prev) return -1;
   Geo g = make_geo(p);
   const long long n = g.n;
   std::vector<double> gi_acc(POG_INLET_NCOEF, 0.0);
@@ -1111,24 +1140,48 @@ extern "C" int orc_adjoint_step_f64(const pog_params* p, const uint32_t* flags, 
           Dual pd[4];
           if (Pd)
             for (int a = 0; a < 4; ++a) pd[a] = Dual((double)Pd[a * n + c]);
-          collide<Dual>(p, g, fl, i, j, k, f, nullptr, Pd ? pd : nullptr, eps != nullptr, e, Dual(0.0), fs,
+          Dual nus(0.0);
+          long long nb[6];
+          const bool st_cell = stencil && les_stencil_cell(g, flags, i, j, k);
+          if (st_cell) {
+            stencil_neighbours(g, i, j, k, nb);
+            Dual un[6][3];
+            for (int m = 0; m < 6; ++m)
+              for (int a = 0; a < 3; ++a) {
+                un[m][a] = Dual(u_prev[a * n + nb[m]]);
+                un[m][a].d[36 + 3 * m + a] = 1.0;
+              }
+            nus = les_nu_from_neighbours<Dual>(p, un);
+          }
+          collide<Dual>(p, g, fl, i, j, k, f, nullptr, Pd ? pd : nullptr, eps != nullptr, e, nus, fs,
                         rho, u, nullptr, coef);
-          for (int q = 0; q < 19; ++q) {
+          // dJ/du of this step's output velocity (stencil mode) joins through u's derivatives
+          double mu[3] = {0, 0, 0};
+          if (stencil && mu_in)
+            for (int a = 0; a < 3; ++a) mu[a] = mu_in[a * n + c];
+          auto pull = [&](int dir) {
             double acc = 0;
-            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[q];
+            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[dir];
+            for (int a = 0; a < 3; ++a) acc += mu[a] * u[a].d[dir];
+            return acc;
+          };
+          for (int q = 0; q < 19; ++q) {
+            double acc = pull(q);
             if (fl & POG_CELL_OUTLET) acc += -(double)CZ[q];
             lam_t[q * n + c] = acc;
           }
-          if (grad_eps && eps) {
-            double acc = 0;
-            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[19];
-            grad_eps[c] += acc;
-          }
-          for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) {
-            double acc = 0;
-            for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[20 + kk];
-            gi[kk] += acc;
-          }
+          if (grad_eps && eps) grad_eps[c] += pull(19);
+          for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) gi[kk] += pull(20 + kk);
+          if (st_cell && mu_out)
+            for (int m = 0; m < 6; ++m)
+              for (int a = 0; a < 3; ++a) {
+                double acc = 0;
+                for (int pq = 0; pq < 19; ++pq) acc += ls[pq] * fs[pq].d[36 + 3 * m + a];
+                if (acc != 0.0) {
+#pragma omp atomic
+                  mu_out[a * n + nb[m]] += acc;
+                }
+              }
         }
 #pragma omp critical
     for (int kk = 0; kk < POG_INLET_NCOEF; ++kk) gi_acc[kk] += gi[kk];

@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .params import INLET_NCOEF, STORE_F32, STORE_F64, LatticeConfig
+from .params import INLET_NCOEF, LES_STENCIL, STORE_F32, STORE_F64, LatticeConfig
 
 _DT = {STORE_F32: torch.float32, STORE_F64: torch.float64}
 
@@ -68,6 +68,18 @@ class OutflowAdjoint:
         self._p = None
         self._eps = None
         self.pc = particles
+        self.stencil = cfg.les_mode == LES_STENCIL
+        # the velocity each step outputs feeds the next step's LES stencil and the particles'
+        # coupling pass: kept as a ping-pong (read / written), checkpointed with the state
+        self._need_u = self.stencil or particles is not None
+        if self._need_u:
+            self._u = torch.zeros((3,) + shape, dtype=torch.float32, device=self.device)
+            self._un = torch.zeros_like(self._u)
+            self._uck = [torch.zeros_like(self._u) for _ in range(self.nseg)]
+        if self.stencil:
+            self._ups = [torch.zeros_like(self._u) for _ in range(self.K)]  # the segment's u_prev
+            self._scratch = torch.empty(int(self.lib.pog_adjoint_scratch_bytes(cfg.to_c())), dtype=torch.uint8,
+                                        device=self.device)
         if particles is not None:
             self._init_particles(particles)
 
@@ -86,8 +98,6 @@ class OutflowAdjoint:
         self._part = [a.clone() for a in self._p0]  # pos, vel, drag_old, active
         self._pck = [[a.clone() for a in self._p0] for _ in range(self.nseg)]
         n = self.cfg.ncell
-        self._u = torch.zeros((3,) + self.shape, dtype=torch.float32, device=dev)
-        self._uck = [torch.zeros_like(self._u) for _ in range(self.nseg)]
         self._fix = torch.zeros(4 * n, dtype=torch.int64, device=dev)
         self._deps = [torch.zeros((4,) + self.shape, dtype=torch.float32, device=dev) for _ in range(self.K)]
         self._dep_hist = None  # all T deposits of the last forward (for loss_frozen), on request
@@ -106,10 +116,16 @@ class OutflowAdjoint:
         c = self.cfg.replace(inlet_coef=tuple(float(x) for x in coef))
         return c.to_c()
 
-    def _push(self, fin, fout, pdrag=None, u_out=None):
+    def _push(self, fin, fout, pdrag=None):
+        """One step fin -> fout; with a velocity history it reads self._u (LES stencil) and writes
+        the step's velocity into self._un, then swaps the two."""
         _lib.check(self.lib.pog_step_push(self._p, _lib.ptr(fin), _lib.ptr(fout), _lib.ptr(self.flags),
-                                          None, _lib.ptr(pdrag), _lib.ptr(self._eps), None, None, _lib.ptr(u_out),
+                                          None, _lib.ptr(pdrag), _lib.ptr(self._eps),
+                                          _lib.ptr(self._u) if self.stencil else None, None,
+                                          _lib.ptr(self._un) if self._need_u else None,
                                           None, _lib.stream_handle()))
+        if self._need_u:
+            self._u, self._un = self._un, self._u
 
     def _start(self, porosity, inlet_coef, initial):
         self._p = self._params(inlet_coef)
@@ -138,10 +154,11 @@ class OutflowAdjoint:
         cur = self._start(porosity, inlet_coef, initial)
         s = _lib.stream_handle()
         nxt = self._states[1] if self.K > 1 else torch.empty_like(cur)
+        if self._need_u:
+            self._u.zero_()  # the velocity before the first step (the solver starts at rest)
         if self.pc is not None:
             for a, b in zip(self._part, self._p0):
                 a.copy_(b)
-            self._u.zero_()
             if record_deposits:
                 self._dep_hist = [torch.empty((4,) + self.shape, dtype=torch.float32, device=self.device)
                                   for _ in range(self.T)]
@@ -150,8 +167,9 @@ class OutflowAdjoint:
             if t % self.K == 0:
                 seg = t // self.K
                 self._ckpt[seg].copy_(cur)
-                if self.pc is not None:
+                if self._need_u:
                     self._uck[seg].copy_(self._u)
+                if self.pc is not None:
                     for a, b in zip(self._pck[seg], self._part):
                         a.copy_(b)
             _lib.check(self.lib.pog_outflow_fixed(self._p, _lib.ptr(cur), _lib.ptr(self.flags), _lib.ptr(self._jfix), s))
@@ -159,7 +177,7 @@ class OutflowAdjoint:
                 self._couple(self._u, dep)
                 if record_deposits:
                     self._dep_hist[t].copy_(dep)
-            self._push(cur, nxt, dep, self._u if self.pc is not None else None)
+            self._push(cur, nxt, dep)
             cur, nxt = nxt, cur
         return self._loss()
 
@@ -171,6 +189,7 @@ class OutflowAdjoint:
         cur = self._start(porosity, inlet_coef, None)
         s = _lib.stream_handle()
         nxt = self._states[1] if self.K > 1 else torch.empty_like(cur)
+        self._u.zero_()
         for t in range(self.T):
             _lib.check(self.lib.pog_outflow_fixed(self._p, _lib.ptr(cur), _lib.ptr(self.flags), _lib.ptr(self._jfix), s))
             self._push(cur, nxt, self._dep_hist[t])
@@ -187,28 +206,38 @@ class OutflowAdjoint:
         g_eps = torch.zeros(self.shape, dtype=torch.float64, device=self.device) \
             if (want_porosity_grad and self._eps is not None) else None
         g_in = torch.zeros(INLET_NCOEF, dtype=torch.float64, device=self.device)
+        # dJ/du of the velocity a step outputs (LES stencil: read by the next step), ping-pong
+        mu = mu_prev = None
+        if self.stencil:
+            mu = torch.zeros((3,) + self.shape, dtype=self.dtype, device=self.device)
+            mu_prev = torch.zeros_like(mu)
         for seg in reversed(range(self.nseg)):
             t0 = seg * self.K
             t1 = min(self.T, t0 + self.K)
             self._states[0].copy_(self._ckpt[seg])
-            if self.pc is not None:
-                # recompute the segment's coupled steps: the same deposits as the forward pass
+            # recompute the segment: the same states, velocities and deposits as the forward pass
+            if self._need_u:
                 self._u.copy_(self._uck[seg])
+            if self.pc is not None:
                 for a, b in zip(self._part, self._pck[seg]):
                     a.copy_(b)
-                for i in range(t1 - t0):
+            for i in range(t1 - t0):
+                if self.stencil:
+                    self._ups[i].copy_(self._u)
+                if self.pc is not None:
                     self._couple(self._u, self._deps[i])
-                    if i + 1 < t1 - t0:
-                        self._push(self._states[i], self._states[i + 1], self._deps[i], self._u)
-            else:
-                for i in range(t1 - t0 - 1):
-                    self._push(self._states[i], self._states[i + 1])
+                if i + 1 < t1 - t0:
+                    self._push(self._states[i], self._states[i + 1], self._deps[i] if self.pc is not None else None)
             for t in reversed(range(t0, t1)):
                 dep = self._deps[t - t0] if self.pc is not None else None
                 _lib.check(self.lib.pog_adjoint_step(
                     self._p, _lib.ptr(self._states[t - t0]), _lib.ptr(lam_next), _lib.ptr(lam_t),
-                    _lib.ptr(self.flags), _lib.ptr(self._eps), _lib.ptr(dep), _lib.ptr(g_eps), _lib.ptr(g_in), s))
+                    _lib.ptr(self.flags), _lib.ptr(self._eps), _lib.ptr(dep),
+                    _lib.ptr(self._ups[t - t0]) if self.stencil else None, _lib.ptr(mu), _lib.ptr(mu_prev),
+                    _lib.ptr(self._scratch) if self.stencil else None, _lib.ptr(g_eps), _lib.ptr(g_in), s))
                 lam_next, lam_t = lam_t, lam_next
+                if self.stencil:
+                    mu, mu_prev = mu_prev, mu
         return AdjointResult(self._loss(), g_eps, g_in)
 
     def loss(self, porosity: Optional[torch.Tensor], inlet_coef) -> float:

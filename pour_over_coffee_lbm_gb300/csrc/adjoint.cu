@@ -13,8 +13,11 @@
 //      u = s(|v|, K(eps), C_F(eps)) v;
 //   3. adds dflux_t/df = -c_z on outlet cells (J = sum_t outflow flux);
 //   4. accumulates dJ/deps (per cell) and dJ/da_k (inlet profile) in FP64.
-// Supported forward configuration: LES off or LOCAL, drag SEMI_IMPLICIT, Guo forcing, no tau
-// clamp, no external force field; a particle drag deposit (Kp, Kv) enters as a fixed input of
+// Supported forward configuration: LES off, LOCAL or STENCIL, drag SEMI_IMPLICIT, Guo forcing, no
+// tau clamp, no external force field.  LES STENCIL: step t's nu_sgs reads the velocity u_{t-1} that
+// step t-1 output, so the adjoint carries dJ/du across steps: reversing step t takes dJ/du_t (its
+// own output velocity, read by step t+1) and returns dJ/du_{t-1} through the transposed central
+// differences (les_grad_vjp_kernel, les_mu_kernel); a particle drag deposit (Kp, Kv) enters as a fixed input of
 // the step (its force Kv - Kp u is differentiated through u, the deposit itself is held).  Gated LES cells (|S| below the floor, nu at its cap) and
 // |u| = 0 points take the zero subgradient.
 #include "collide.cuh"
@@ -70,10 +73,11 @@ __device__ __forceinline__ void eq_vjp_diff(const C a[19], const C b[19], C rho,
 // Inlet cell c (f* = feq(rho, (0, 0, u_z(a)))): bar f (all directions equal) from the pulled
 // lam*, and the cell's contributions to dJ/da_k added into g[16].
 template <typename C>
-__device__ __forceinline__ C adj_inlet_cell(const KParams& kp, uint32_t c, const C ls[19], C rho, double g[16]) {
+__device__ __forceinline__ C adj_inlet_cell(const KParams& kp, uint32_t c, const C ls[19], C rho, C mu_z, double g[16]) {
   const C uz = inlet_uz<C>(kp, c);
   C brho, bux, buy, buz;
   eq_vjp<C>(ls, rho, (C)0, (C)0, uz, brho, bux, buy, buz);
+  buz += mu_z;  // the cell's output velocity (0, 0, u_z) read by the next step's LES stencil
   // uz = u_inlet (1 + sum a_k T_k(s)), s = 2 r / R - 1
   const uint32_t i = c % kp.nx, j = (c / kp.nx) % kp.ny;
   const C dx = (C)i - (C)kp.cxf, dy = (C)j - (C)kp.cyf;
@@ -114,7 +118,8 @@ template <int S>
 __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
-    const uint32_t* __restrict__ flags, uint32_t lo, uint32_t hi, double* __restrict__ grad_inlet) {
+    const uint32_t* __restrict__ flags, uint32_t lo, uint32_t hi, const typename Store<S>::E* __restrict__ mu_in,
+    double* __restrict__ grad_inlet) {
   using St = Store<S>;
   using C = typename St::C;
   using E = typename St::E;
@@ -130,7 +135,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
     C rho = 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) rho += St::ld(ft, (uint32_t)q * n + c, q, (C)kp.rho0);
-    const C brho = adj_inlet_cell<C>(kp, c, ls, rho, g);
+    const C brho = adj_inlet_cell<C>(kp, c, ls, rho, mu_in ? (C)mu_in[2u * n + c] : (C)0, g);
 #pragma unroll
     for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)brho;
   }
@@ -157,7 +162,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
     const uint32_t* __restrict__ flags, const float* __restrict__ eps, const float* __restrict__ pdrag,
-    double* __restrict__ grad_eps, double* __restrict__ grad_inlet, uint32_t inlet_lo, uint32_t inlet_hi) {
+    const float* __restrict__ u_prev, const typename Store<S>::E* __restrict__ mu_in,
+    typename Store<S>::C* __restrict__ bar_nu, double* __restrict__ grad_eps, double* __restrict__ grad_inlet,
+    uint32_t inlet_lo, uint32_t inlet_hi) {
   using St = Store<S>;
   using C = typename St::C;
   using E = typename St::E;
@@ -168,11 +175,15 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
   __syncthreads();
   for (uint32_t c = blockIdx.x * ADJ_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_BLOCK) {
     const uint32_t fl = flags[c];
+    if (bar_nu) bar_nu[c] = (C)0;  // dJ/dnu of the cells whose stencil nu is live, below
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)0;
       continue;
     }
+    // dJ/du of the velocity this step outputs (read by the next step's LES stencil)
+    const C mux = mu_in ? (C)mu_in[c] : (C)0, muy = mu_in ? (C)mu_in[n + c] : (C)0,
+            muz = mu_in ? (C)mu_in[2u * n + c] : (C)0;
     // the inlet plane's inlet cells are done by adjoint_inlet_kernel
     if ((fl & POG_CELL_INLET) && c >= inlet_lo && c < inlet_hi) continue;
     // 1. transpose of push streaming
@@ -196,7 +207,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       double g[POG_INLET_NCOEF];
 #pragma unroll
       for (int k = 0; k < POG_INLET_NCOEF; ++k) g[k] = 0.0;
-      brho = adj_inlet_cell<C>(kp, c, ls, rho, g);
+      brho = adj_inlet_cell<C>(kp, c, ls, rho, muz, g);
 #pragma unroll
       for (int k = 0; k < POG_INLET_NCOEF; ++k) atomicAdd(&ginl[k], g[k]);
 #pragma unroll
@@ -206,6 +217,9 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       C br_out, bux, buy, buz;
       eq_vjp<C>(ls, (C)kp.rho_out, ux, uy, uz, br_out, bux, buy, buz);
       (void)br_out;
+      bux += mux;
+      buy += muy;
+      buz += muz;
       bmx = bux / rho;
       bmy = buy / rho;
       bmz = buz / rho;
@@ -270,6 +284,17 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       const C tau0 = (C)kp.tau;
       C tau = tau0;
       bool les_live = false;
+      bool st_live = false;  // the stencil nu is in its linear range (not gated, not capped)
+      if (kp.les_mode == POG_LES_STENCIL && !porous) {
+        C gr[9];
+        les_stencil_grad<C>(kp, c, u_prev, gr);
+        const C smag = les_smag<C>(gr);
+        if (!(smag < (C)kp.strain_floor)) {
+          const C nu = (C)kp.cs2 * smag;
+          st_live = nu < (C)kp.nu_max;
+          tau = tau0 + (C)3 * (st_live ? nu : (C)kp.nu_max);
+        }
+      }
       C Pxx = 0, Pyy = 0, Pzz = 0, Pxy = 0, Pxz = 0, Pyz = 0, Q = 0, Rr = 0;
       if (kp.les_mode == POG_LES_LOCAL && !porous) {
 #pragma unroll
@@ -328,6 +353,11 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       }
       bomega += (C)-0.5 * bA;
       const C btau = -bomega / (tau * tau);
+      if (st_live && bar_nu) bar_nu[c] = (C)3 * btau;
+      // this cell's output velocity is u: dJ/du from the next step's stencil joins here
+      bux += mux;
+      buy += muy;
+      buz += muz;
       if (les_live) {
         const C bnu = (C)3 * btau;
         const C btl = bnu / (C)3;
@@ -430,9 +460,61 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
   }
 }
 
+// dJ/dnu -> dJ/d(grad u) of each cell's stencil (nu = cs^2 |S|, |S| = sqrt(2 P), P the strain
+// invariant of the central-difference gradient): bar_g[3 a + b] = dJ/d(du_a/dx_b), 0 where the
+// stencil is not live (bar_nu 0).
+template <typename C>
+__global__ void les_grad_vjp_kernel(const KParams kp, const float* __restrict__ u_prev, const C* __restrict__ bar_nu,
+                                    C* __restrict__ bar_g) {
+  const uint32_t n = kp.n;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    C out[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const C bn = bar_nu[c];
+    if (bn != (C)0 && c >= kp.guard_lo && c <= kp.guard_hi) {
+      C g[9];
+      les_stencil_grad<C>(kp, c, u_prev, g);
+      const C smag = les_smag<C>(g);
+      const C bP = bn * (C)kp.cs2 / smag;  // d|S|/dP = 1/|S|
+      const C s12 = (C)0.5 * (g[1] + g[3]), s13 = (C)0.5 * (g[2] + g[6]), s23 = (C)0.5 * (g[5] + g[7]);
+      out[0] = bP * (C)2 * g[0];
+      out[4] = bP * (C)2 * g[4];
+      out[8] = bP * (C)2 * g[8];
+      out[1] = out[3] = bP * (C)2 * s12;
+      out[2] = out[6] = bP * (C)2 * s13;
+      out[5] = out[7] = bP * (C)2 * s23;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) bar_g[(uint32_t)k * n + c] = out[k];
+  }
+}
+
+// dJ/du_prev(x)_a = sum_b (bar_g_ab(x - e_b) - bar_g_ab(x + e_b)) / 2: the transpose of the
+// central differences du_a/dx_b(y) = (u_a(y + e_b) - u_a(y - e_b)) / 2.
+template <typename C, typename E>
+__global__ void les_mu_kernel(const KParams kp, const C* __restrict__ bar_g, E* __restrict__ mu_out) {
+  const uint32_t n = kp.n;
+  const uint32_t st[3] = {1u, kp.nx, kp.nxny};
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const bool in = c >= kp.nxny && c + kp.nxny < n;  // both neighbours along every axis exist
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      C m = 0;
+      if (in) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          const C* g = bar_g + (uint32_t)(3 * a + b) * n;
+          m += (C)0.5 * (g[c - st[b]] - g[c + st[b]]);
+        }
+      }
+      mu_out[(uint32_t)a * n + c] = (E)m;
+    }
+  }
+}
+
 template <int S>
 static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* lt, const uint32_t* flags,
-                      const float* eps, const float* pdrag, double* ge, double* gi, cudaStream_t s) {
+                      const float* eps, const float* pdrag, const float* u_prev, const void* mu_in, void* mu_out,
+                      void* scratch, double* ge, double* gi, cudaStream_t s) {
   auto kern = adjoint_kernel<S>;
   static thread_local int grid = 0;
   if (grid == 0) grid = persistent_blocks((const void*)kern, ADJ_BLOCK);
@@ -440,13 +522,24 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
   int want = (int)((kp.n + ADJ_BLOCK - 1) / ADJ_BLOCK);
   int g = want < grid ? want : grid;
   using E = typename Store<S>::E;
+  using C = typename Store<S>::C;
   const uint32_t lo = (kp.nz - 2u) * kp.nxny, hi = lo + kp.nxny;  // the inlet plane
-  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, pdrag, ge, gi, lo, hi);
+  C* bar_nu = scratch ? (C*)scratch : nullptr;
+  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, pdrag, u_prev, (const E*)mu_in,
+                               bar_nu, ge, gi, lo, hi);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
-  adjoint_inlet_kernel<S><<<1, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi, gi);
+  adjoint_inlet_kernel<S><<<1, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi,
+                                                  (const E*)mu_in, gi);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
+  if (scratch && mu_out) {
+    C* bar_g = bar_nu + kp.n;
+    les_grad_vjp_kernel<C><<<g, ADJ_BLOCK, 0, s>>>(kp, u_prev, bar_nu, bar_g);
+    les_mu_kernel<C, E><<<g, ADJ_BLOCK, 0, s>>>(kp, bar_g, (E*)mu_out);
+    count_launch(2);
+    POG_TRY_CUDA(cudaGetLastError());
+  }
   return POG_OK;
 }
 
@@ -498,15 +591,30 @@ extern "C" int pog_outflow_fixed(const pog_params* p, const void* f_nat, const u
   return POG_OK;
 }
 
+extern "C" size_t pog_adjoint_scratch_bytes(const pog_params* p) {
+  if (!p || p->les_mode != POG_LES_STENCIL) return 0;
+  const size_t n = (size_t)p->nx * p->ny * p->nz;
+  return 10 * n * (p->storage == POG_STORE_F64 ? sizeof(double) : sizeof(float));
+}
+
 extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next,
                                 void* lam_t, const uint32_t* flags, const float* porosity, const float* pdrag,
+                                const float* u_prev, const void* dJ_du, void* dJ_du_prev, void* scratch,
                                 double* grad_porosity, double* grad_inlet, void* stream) {
   int rc = pog_validate_params(p);
   if (rc) return rc;
   if (!f_t || !lam_next || !lam_t || !flags) return set_error(POG_E_ARG, "NULL pointer");
   if (lam_next == lam_t) return set_error(POG_E_ARG, "lam_next and lam_t must differ");
-  if (p->les_mode == POG_LES_STENCIL)
-    return set_error(POG_E_ARG, "adjoint supports les_mode OFF or LOCAL");
+  const bool stencil = p->les_mode == POG_LES_STENCIL;
+  if (stencil && (!u_prev || !dJ_du_prev || !scratch))
+    return set_error(POG_E_ARG, "LES stencil mode needs u_prev, dJ_du_prev and scratch");
+  if (stencil && dJ_du == dJ_du_prev) return set_error(POG_E_ARG, "dJ_du and dJ_du_prev must differ");
+  if (!stencil) {
+    u_prev = nullptr;
+    dJ_du = nullptr;
+    dJ_du_prev = nullptr;
+    scratch = nullptr;
+  }
   if (p->drag_mode != POG_DRAG_SEMI_IMPLICIT || p->forcing_mode != POG_FORCING_GUO || p->clamp_tau)
     return set_error(POG_E_ARG, "adjoint supports semi-implicit drag, Guo forcing, no tau clamp");
   if (grad_porosity && !porosity) return set_error(POG_E_ARG, "grad_porosity needs porosity");
@@ -515,8 +623,10 @@ extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void
   KParams kp = make_kparams(p);
   cudaStream_t s = (cudaStream_t)stream;
   if (p->storage == POG_STORE_F32)
-    return launch_adj<POG_STORE_F32>(kp, f_t, lam_next, lam_t, flags, porosity, pdrag, grad_porosity, grad_inlet, s);
+    return launch_adj<POG_STORE_F32>(kp, f_t, lam_next, lam_t, flags, porosity, pdrag, u_prev, dJ_du, dJ_du_prev,
+                                     scratch, grad_porosity, grad_inlet, s);
   if (p->storage == POG_STORE_F64)
-    return launch_adj<POG_STORE_F64>(kp, f_t, lam_next, lam_t, flags, porosity, pdrag, grad_porosity, grad_inlet, s);
+    return launch_adj<POG_STORE_F64>(kp, f_t, lam_next, lam_t, flags, porosity, pdrag, u_prev, dJ_du, dJ_du_prev,
+                                     scratch, grad_porosity, grad_inlet, s);
   return set_error(POG_E_ARG, "adjoint storage must be F32 or F64");
 }

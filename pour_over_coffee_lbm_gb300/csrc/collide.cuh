@@ -401,24 +401,35 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   return res;
 }
 
-// LES nu_sgs from central differences of the previous step's velocity u[3][n]
+// Central-difference velocity gradient of cell c from u[3][n]: g[3 a + b] = du_a/dx_b
 // (les_turbulence.py:318-380).  Fluid cells are interior, so the 6 neighbours exist.
+template <typename C>
+__host__ __device__ __forceinline__ void les_stencil_grad(const KParams& kp, uint32_t c, const float* __restrict__ u,
+                                                         C g[9]) {
+  const uint32_t n = kp.n, st[3] = {1u, kp.nx, kp.nxny};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float* v = u + (uint32_t)a * n;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) g[3 * a + b] = ((C)v[c + st[b]] - (C)v[c - st[b]]) * (C)0.5;
+  }
+}
+
+// |S| = sqrt(2 S:S) of a gradient g (S the symmetric part).
+template <typename C>
+__host__ __device__ __forceinline__ C les_smag(const C g[9]) {
+  const C S12 = (C)0.5 * (g[1] + g[3]), S13 = (C)0.5 * (g[2] + g[6]), S23 = (C)0.5 * (g[5] + g[7]);
+  return sqrt((C)2 * (g[0] * g[0] + g[4] * g[4] + g[8] * g[8] + (C)2 * (S12 * S12 + S13 * S13 + S23 * S23)));
+}
+
+// LES nu_sgs from central differences of the previous step's velocity u[3][n]
+// (les_turbulence.py:318-380): nu = min(cs^2 |S|, nu_max), zero below the strain floor.
 template <typename C>
 __host__ __device__ __forceinline__ C les_nu_stencil(const KParams& kp, uint32_t c,
                                                      const float* __restrict__ u) {
-  const uint32_t n = kp.n, sx = 1, sy = kp.nx, sz = kp.nxny;
-  const float* ux = u;
-  const float* uy = u + n;
-  const float* uz = u + 2u * n;
-  C dudx = ((C)ux[c + sx] - (C)ux[c - sx]) * (C)0.5, dudy = ((C)ux[c + sy] - (C)ux[c - sy]) * (C)0.5,
-    dudz = ((C)ux[c + sz] - (C)ux[c - sz]) * (C)0.5;
-  C dvdx = ((C)uy[c + sx] - (C)uy[c - sx]) * (C)0.5, dvdy = ((C)uy[c + sy] - (C)uy[c - sy]) * (C)0.5,
-    dvdz = ((C)uy[c + sz] - (C)uy[c - sz]) * (C)0.5;
-  C dwdx = ((C)uz[c + sx] - (C)uz[c - sx]) * (C)0.5, dwdy = ((C)uz[c + sy] - (C)uz[c - sy]) * (C)0.5,
-    dwdz = ((C)uz[c + sz] - (C)uz[c - sz]) * (C)0.5;
-  C S12 = (C)0.5 * (dudy + dvdx), S13 = (C)0.5 * (dudz + dwdx), S23 = (C)0.5 * (dvdz + dwdy);
-  C smag = sqrt((C)2 * (dudx * dudx + dvdy * dvdy + dwdz * dwdz +
-                        (C)2 * (S12 * S12 + S13 * S13 + S23 * S23)));
+  C g[9];
+  les_stencil_grad<C>(kp, c, u, g);
+  const C smag = les_smag<C>(g);
   if (smag < (C)kp.strain_floor) return (C)0;
   C nu = (C)kp.cs2 * smag;
   return nu < (C)kp.nu_max ? nu : (C)kp.nu_max;

@@ -113,12 +113,70 @@ def test_autograd_function_and_fp32(cuda):
 
 def test_adjoint_rejects_unsupported_modes(cuda):
     from pour_over_coffee_lbm_gb300 import _lib
-    from pour_over_coffee_lbm_gb300.params import LES_STENCIL
-    cfg = _case().replace(storage=STORE_F64, les_mode=LES_STENCIL)
+    from pour_over_coffee_lbm_gb300.params import DRAG_EXPLICIT_CAP
+    cfg = _case().replace(storage=STORE_F64, drag_mode=DRAG_EXPLICIT_CAP)
     run = OutflowAdjoint(cfg, steps=2, checkpoint_every=1)
     with pytest.raises(_lib.PogError):
         run.forward(None, cfg.inlet_coef)
         run.backward()
+
+
+def _stencil_case():
+    from pour_over_coffee_lbm_gb300.params import LES_STENCIL
+    # the reference-faithful LES: nu_sgs from central differences of the previous step's u
+    return _case().replace(storage=STORE_F64, les_mode=LES_STENCIL, cs_smag=0.4)
+
+
+def test_stencil_adjoint_matches_dual_number_oracle(cuda, orc):
+    """LES stencil mode (les_turbulence.py:318-380): dJ/du crosses steps through the stencil; the
+    GPU adjoint equals the oracle's dual-number adjoint, which seeds the six neighbours'
+    velocities as directions and carries the same velocity adjoint back."""
+    cfg = _stencil_case()
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps_np = porosity_field(cfg, fl, seed=5)
+    eps = torch.as_tensor(eps_np).reshape(cfg.nz, cfg.ny, cfg.nx)
+    T = 14
+    run = OutflowAdjoint(cfg, steps=T, checkpoint_every=4)
+    run.forward(eps, cfg.inlet_coef)
+    res = run.backward()
+    ge, gi = orc.outflow_gradient(cfg, T, flags=fl, eps=eps_np.reshape(cfg.nz, cfg.ny, cfg.nx))
+    gin = res.grad_inlet.cpu().numpy()
+    assert np.abs(gin - gi).max() <= 1e-7 * np.abs(gi).max()
+    g_gpu = res.grad_porosity.cpu().numpy()
+    assert np.abs(g_gpu - ge).max() <= 1e-7 * np.abs(ge).max()
+    # checkpoint spacing does not change the result
+    one = OutflowAdjoint(cfg, steps=T, checkpoint_every=T)
+    one.forward(eps, cfg.inlet_coef)
+    r1 = one.backward()
+    assert torch.equal(r1.grad_inlet, res.grad_inlet) and torch.equal(r1.grad_porosity, res.grad_porosity)
+
+
+def test_stencil_adjoint_finite_differences(cuda):
+    cfg = _stencil_case().replace(nx=20, ny=20, nz=20, cone_apex_z=3.0, inlet_radius=5.0)
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=25)).reshape(cfg.nz, cfg.ny, cfg.nx)
+    run = OutflowAdjoint(cfg, steps=40, checkpoint_every=10)
+    run.forward(eps, cfg.inlet_coef)
+    res = run.backward()
+    h = 1e-3
+    coef = np.array(cfg.inlet_coef, np.float64)
+    for k in (0, 1, 5, 15):
+        cp = coef.copy(); cp[k] += h
+        cm = coef.copy(); cm[k] -= h
+        fd = (run.loss(eps, cp) - run.loss(eps, cm)) / (2 * h)
+        ad = res.grad_inlet[k].item()
+        assert abs(ad - fd) <= 1e-4 * abs(fd) + 1e-14, (k, ad, fd)
+    ge = res.grad_porosity.cpu().numpy().reshape(-1)
+    band = np.flatnonzero((fl.reshape(-1) & CELL_POROUS) != 0)
+    flat = eps.reshape(-1)
+    for c in band[np.argsort(-np.abs(ge[band]))[:6]]:
+        ep = flat.clone(); ep[c] += h
+        em = flat.clone(); em[c] -= h
+        hh = (ep[c].double() - em[c].double()).item() / 2
+        fd = (run.loss(ep.reshape(eps.shape), coef) - run.loss(em.reshape(eps.shape), coef)) / (2 * hh)
+        assert abs(ge[c] - fd) <= 1e-4 * abs(fd), (c, ge[c], fd)
 
 
 def test_forward_from_a_given_state(cuda):

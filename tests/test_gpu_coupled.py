@@ -13,9 +13,10 @@ Bars:
 - one coupling pass, deterministic (fixed-point) deposit, same input state on both sides: every
   particle output and the deposit bit-exact against the oracle;
 - 100 coupled steps (GB300LBMSolver.step_with_two_way_coupling against the oracle's coupled
-  sequence): the fluid and the particles drift apart only by FP32 rounding of the lattice (the
-  GPU stores shifted FP32, the FP32 oracle plain FP32): u within 1e-4 relative L2, particle
-  positions within 1e-3 cells for 99.9 % of the particles and 1e-5 in the median;
+  sequence with an FP64 lattice): the fluid and the particles drift apart only by the GPU's FP32
+  rounding of the lattice (it stores the shifted deviations, and sits near FP64; the plain-FP32
+  oracle is itself ~2e-4 from FP64 in u here, so it is not the yardstick): u within 1e-5 relative
+  L2, particle positions within 1e-3 cells for 99.9 % of the particles and 1e-5 in the median;
 - fast (float atomics) against deterministic deposit on the GPU: the same bars.
 The explicit exchange is stable at this loading (the test asserts it); where it is not is stated
 in the design notes (the implicit exchange is the default for that reason)."""
@@ -88,24 +89,27 @@ def _coupled_run_gpu(pc, steps):
 
 
 def _coupled_run_oracle(orc, pc, steps):
+    """The oracle's coupled sequence with an FP64 lattice (the particle pass is FP32, fed the
+    lattice velocity rounded to FP32 as the GPU feeds it)."""
     flags = orc.build_flags(C2)
-    f = orc.init_equilibrium(C2, flags, np.float32)
+    f = orc.init_equilibrium(C2.replace(storage=3), flags, np.float64)
     pos, vel, d, act = seed_particles(C2, pc)
     drag = np.zeros_like(pos)
-    _, _, u = orc.step(C2, flags, f)
+    u = np.zeros((3, C2.nz, C2.ny, C2.nx), np.float32)
     for _ in range(steps):
         pos, vel, drag, act, fix, _ = orc.particles_couple(C2, pc, pos, vel, d, drag, act, u)
         pdrag = (fix.astype(np.float64) / 2.0 ** 32).astype(np.float32).reshape(4, C2.nz, C2.ny, C2.nx)
-        f, rho, u = orc.step(C2, flags, f, pdrag=pdrag)
+        f, rho, u64 = orc.step(C2.replace(storage=3), flags, f, pdrag=pdrag)
+        u = u64.astype(np.float32)
     return flags, u, pos, act
 
 
-def _compare(gu, gpos, u, pos, fluid, label):
+def _compare(gu, gpos, u, pos, fluid, label, bar=1e-5):
     e = np.linalg.norm(gu[:, fluid] - u[:, fluid]) / np.linalg.norm(u[:, fluid])
     dp = np.abs(gpos - pos).max(0)
     print("%s: u rel L2 %.2e; particle |dx| median %.1e, 99.9%% %.1e, max %.1e"
           % (label, e, np.median(dp), np.quantile(dp, 0.999), dp.max()))
-    assert e < 1e-4
+    assert e < bar
     assert np.median(dp) < 1e-5 and np.quantile(dp, 0.999) < 1e-3
     return e
 

@@ -88,7 +88,8 @@ def test_adjoint_rejects_blockage(cuda):
     f = torch.zeros((19, cfg.ncell), dtype=torch.float32, device="cuda")
     lam = torch.zeros_like(f)
     fl = torch.zeros(cfg.ncell, dtype=torch.int32, device="cuda")
-    rc = lib().pog_adjoint_step(ctypes.byref(p), P(f), P(lam), P(torch.zeros_like(f)), P(fl), None, None, None, None, S())
+    rc = lib().pog_adjoint_step(ctypes.byref(p), P(f), P(lam), P(torch.zeros_like(f)), P(fl), None, None, None, None,
+                                None, None, None, None, S())
     assert rc != 0
 
 
