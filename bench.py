@@ -53,8 +53,9 @@ def parse():
     ap.add_argument("--precision-case", choices=["les_band", "plain"], default="les_band")
     ap.add_argument("--scale-only", action="store_true",
                     help="run --steps coupled steps of the 320x320x384 / 1M-particle case (profiling)")
-    ap.add_argument("--step-kernel", choices=["rows", "registers"], default="registers",
-                    help="lattice step kernel: row-tiled TMA-staged, or register-staged")
+    ap.add_argument("--step-kernel", choices=["auto", "rows", "registers"], default="auto",
+                    help="lattice step kernel: auto (two-cell kernel for 16-bit storage, else per-cell), "
+                         "row-tiled TMA-staged, or per-cell register-staged")
     return ap.parse_args()
 
 
@@ -154,7 +155,7 @@ def time_graph(graph, replays):
     return start.elapsed_time(end) / 1e3
 
 
-def kernel_roofline(cfg, pc, steps, peak, step_kernel="registers"):
+def kernel_roofline(cfg, pc, steps, peak, step_kernel="auto"):
     """Average duration of the fused LBM step kernel alone with the arguments it has inside the
     coupled step (the particle drag deposit and its cell mask of a real coupling pass, rho/u
     written), over `steps` graph-replayed launches."""
@@ -428,7 +429,7 @@ def differentiation_rows(peak):
     return out
 
 
-def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="registers"):
+def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="auto"):
     """320x320x384 FP16S + LES + band + 1,000,000 particles: exactly `steps` two-way coupled steps
     (4 eager, the rest graph-replayed), then the outflow adjoint over the last adj_steps of them
     (recomputed in FP32 from the FP16S state exported at step steps - adj_steps, checkpoints every
@@ -554,7 +555,7 @@ def precision_cfg(storage, case):
                          band=kw.get("band", 3.0))
 
 
-def precision_line(storage, steps, peak, case="les_band", step_kernel="registers"):
+def precision_line(storage, steps, peak, case="les_band", step_kernel="auto"):
     import torch
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     cfg = precision_cfg(storage, case)
@@ -876,7 +877,8 @@ def run_ours(args):
     if os.path.exists(traffic_path):
         with open(traffic_path) as fh:
             tr = json.load(fh)
-        key = "les_band 256x256x256 fp32 %s" % args.step_kernel
+        # FP32 storage: "auto" runs the per-cell register-staged kernel
+        key = "les_band 256x256x256 fp32 %s" % ("registers" if args.step_kernel == "auto" else args.step_kernel)
         if key in tr:
             h["roofline"]["traffic"] = tr[key]["bytes_per_step"]
             h["roofline"]["traffic_source"] = tr[key].get("source")
@@ -889,7 +891,8 @@ def run_ours(args):
                             ("plain", "256^3 D3Q19, gravity + inlet/outlet + cone walls (no LES, no band)")):
             lines = {}
             for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
-                lines[name] = {k: precision_line(st, 200, peak, case, k) for k in ("rows", "registers")}
+                kernels = ("rows", "registers") if st == STORE_F32 else ("rows", "registers", "auto")
+                lines[name] = {k: precision_line(st, 200, peak, case, k) for k in kernels}
             best = {n: max(v.values(), key=lambda d: d["mlups"]) for n, v in lines.items()}
             errs = precision_errors(args.error_steps, case) if args.error_steps > 0 else None
             extra[case] = {"workload": label, "lines": lines, "error_vs_fp64": errs,

@@ -147,7 +147,17 @@ typedef struct pog_params {
    * compute the same update and leave the same state between steps. */
   const int32_t* wall_cells;
   int32_t n_wall_cells;
+  /* enum pog_step_kernel: which register-staged step kernel pog_step runs when wall_cells is NULL.
+   * POG_STEP_AUTO: FP16S/BF16S storage takes the two-cell kernel (two x-adjacent cells per
+   * thread, paired 32-bit population accesses, packed FP32x2 collision) where it applies -- even
+   * nx, Guo forcing, no phase field, LES off or local -- and every other case the per-cell
+   * kernel.  POG_STEP_CELLS: the per-cell kernel always.  Both compute the same update; the
+   * two-cell kernel's collision rounds differently in FP32, so 16-bit stored values can differ
+   * by one unit in their last place. */
+  int32_t step_kernel;
 } pog_params;
+
+enum pog_step_kernel { POG_STEP_AUTO = 0, POG_STEP_CELLS = 1 };
 
 /* Pour-nozzle block, floats (PrecisePouringSystem, src/physics/precise_pouring.py:12-193):
  * a stream of radius R ending at plane ZTOP, HEIGHT planes tall, centred at (X, Y).  A fluid cell

@@ -22,6 +22,7 @@ SOURCES = {
     "geometry.cu": ["-fmad=false"],
     "lbm_aa.cu": FAST_F32,
     "lbm_tma.cu": FAST_F32,
+    "lbm_pair.cu": FAST_F32,
     "lbm_push.cu": [],
     "particles.cu": ["-fmad=false"],
     "particles_noalloc.cu": [],

@@ -139,6 +139,8 @@ int pog_validate_params(const pog_params* p) {
     return set_error(POG_E_ARG, "cone half angle must be in (0, 89) degrees");
   if (p->wall_cells && p->n_wall_cells < 0)
     return set_error(POG_E_ARG, "n_wall_cells=%d must be >= 0", p->n_wall_cells);
+  if (p->step_kernel != POG_STEP_AUTO && p->step_kernel != POG_STEP_CELLS)
+    return set_error(POG_E_ARG, "step_kernel=%d unknown", p->step_kernel);
   if (p->clamp_tau && !(p->tau_min > 0.5f && p->tau_max >= p->tau_min))
     return set_error(POG_E_ARG, "tau clamp [%g,%g] invalid", (double)p->tau_min, (double)p->tau_max);
   return POG_OK;

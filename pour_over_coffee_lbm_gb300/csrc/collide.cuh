@@ -151,6 +151,72 @@ __device__ __forceinline__ void collide_pair2(C f[19], C ux, C uy, C uz, C Fx, C
   f[P2] = FP.y;
 }
 
+// Velocity and total force of a cell of the filter-paper band (filter_paper.py:471-536): the
+// Darcy-Forchheimer drag rho (nu/K + C_F |u| / sqrt K) u, semi-implicit (Guo & Zhao 2002, solved
+// in closed form) or explicit and capped (POG_DRAG_EXPLICIT_CAP), with the particle deposit
+// (Kp, Kv) implicit.  On entry u = (m + (G + Kv)/2) / rho, the velocity with every explicit force
+// and A = 1 + Kp/(2 rho) not yet divided out; on exit u and F are the cell's collision velocity
+// and force density.
+template <typename C>
+__host__ __device__ __forceinline__ void porous_drag(const KParams& kp, uint32_t c, const float* __restrict__ eps,
+                                                     C rho, C inv_rho, C A, C Kp, C Kvx, C Kvy, C Kvz, C Gx,
+                                                     C Gy, C Gz, C mx, C my, C mz, C& ux, C& uy, C& uz, C& Fx,
+                                                     C& Fy, C& Fz) {
+  C K = (C)kp.K0, CF = (C)kp.CF0;
+  if (eps) {
+    C e = (C)eps[c];
+    C g = e * e * e / (((C)1 - e) * ((C)1 - e));
+    K = (C)kp.K0 * (g / (C)kp.g0);
+    C r = (C)kp.eps0 / e;
+    CF = (C)kp.CF0 * (r * sqrt(r));
+  }
+  // Darcy nu/K and Forchheimer C_F/sqrt(K) coefficients, both scaled by the filter
+  // blockage factor 1 + b when a blockage field is given
+  C dk = (C)kp.nu0 / K, fk = CF / sqrt(K);
+  if (kp.blockage) {
+    const C bf = (C)1 + (C)kp.blockage[c];
+    dk *= bf;
+    fk *= bf;
+  }
+  if (kp.drag_mode == POG_DRAG_SEMI_IMPLICIT) {
+    // Guo & Zhao 2002: u (A + nu/(2K) + C_F|u|/(2 sqrt K)) = v, solved in closed form.
+    C c0 = (C)0.5 * (A + (C)0.5 * dk);
+    C c1 = (C)0.5 * fk;
+    C vm = sqrt(ux * ux + uy * uy + uz * uz);
+    C s = (C)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
+    ux *= s;
+    uy *= s;
+    uz *= s;
+    C um = sqrt(ux * ux + uy * uy + uz * uz);
+    C coef = rho * (dk + fk * um) + Kp;
+    Fx = Gx + Kvx - coef * ux;
+    Fy = Gy + Kvy - coef * uy;
+    Fz = Gz + Kvz - coef * uz;
+  } else {
+    ux /= A;
+    uy /= A;
+    uz /= A;
+    C vm = sqrt(ux * ux + uy * uy + uz * uz);
+    C coef = rho * (dk + fk * vm);
+    C dx = -coef * ux, dy = -coef * uy, dz = -coef * uz;
+    C dm = sqrt(dx * dx + dy * dy + dz * dz);
+    C cap = (C)kp.drag_cap;
+    if (dm > cap) {
+      C sc = cap / dm;
+      dx *= sc;
+      dy *= sc;
+      dz *= sc;
+    }
+    // capped drag as an explicit force, particle drag implicit: u A = (m + (G + Kv + F_d)/2)/rho
+    ux = (mx + (C)0.5 * (Gx + Kvx + dx)) * inv_rho / A;
+    uy = (my + (C)0.5 * (Gy + Kvy + dy)) * inv_rho / A;
+    uz = (mz + (C)0.5 * (Gz + Kvz + dz)) * inv_rho / A;
+    Fx = Gx + dx + Kvx - Kp * ux;
+    Fy = Gy + dy + Kvy - Kp * uy;
+    Fz = Gz + dz + Kvz - Kp * uz;
+  }
+}
+
 // f[19]: incoming populations on entry, post-collision populations on exit.
 // SH (shifted): f holds h_q = (f_q - w_q rs) / sc instead of f_q, in and out -- the form the
 // shifted storages keep, rs = the cell's shift density.  Moments, Pi_neq and the post-collision
@@ -239,59 +305,8 @@ __host__ __device__ __forceinline__ CellResult<C> collide_cell(const KParams& kp
   C Fx = Gx, Fy = Gy, Fz = Gz;
   const bool porous = (fl & POG_CELL_POROUS) != 0;
   if (porous) {
-    C K = (C)kp.K0, CF = (C)kp.CF0;
-    if (eps) {
-      C e = (C)eps[c];
-      C g = e * e * e / (((C)1 - e) * ((C)1 - e));
-      K = (C)kp.K0 * (g / (C)kp.g0);
-      C r = (C)kp.eps0 / e;
-      CF = (C)kp.CF0 * (r * sqrt(r));
-    }
-    // Darcy nu/K and Forchheimer C_F/sqrt(K) coefficients, both scaled by the filter
-    // blockage factor 1 + b when a blockage field is given
-    C dk = (C)kp.nu0 / K, fk = CF / sqrt(K);
-    if (kp.blockage) {
-      const C bf = (C)1 + (C)kp.blockage[c];
-      dk *= bf;
-      fk *= bf;
-    }
-    if (kp.drag_mode == POG_DRAG_SEMI_IMPLICIT) {
-      // Guo & Zhao 2002: u (A + nu/(2K) + C_F|u|/(2 sqrt K)) = v, solved in closed form.
-      C c0 = (C)0.5 * (A + (C)0.5 * dk);
-      C c1 = (C)0.5 * fk;
-      C vm = sqrt(ux * ux + uy * uy + uz * uz);
-      C s = (C)1 / (c0 + sqrt(c0 * c0 + c1 * vm));
-      ux *= s;
-      uy *= s;
-      uz *= s;
-      C um = sqrt(ux * ux + uy * uy + uz * uz);
-      C coef = rho * (dk + fk * um) + Kp;
-      Fx = Gx + Kvx - coef * ux;
-      Fy = Gy + Kvy - coef * uy;
-      Fz = Gz + Kvz - coef * uz;
-    } else {
-      ux /= A;
-      uy /= A;
-      uz /= A;
-      C vm = sqrt(ux * ux + uy * uy + uz * uz);
-      C coef = rho * (dk + fk * vm);
-      C dx = -coef * ux, dy = -coef * uy, dz = -coef * uz;
-      C dm = sqrt(dx * dx + dy * dy + dz * dz);
-      C cap = (C)kp.drag_cap;
-      if (dm > cap) {
-        C sc = cap / dm;
-        dx *= sc;
-        dy *= sc;
-        dz *= sc;
-      }
-      // capped drag as an explicit force, particle drag implicit: u A = (m + (G + Kv + F_d)/2)/rho
-      ux = (mx + (C)0.5 * (Gx + Kvx + dx)) * inv_rho / A;
-      uy = (my + (C)0.5 * (Gy + Kvy + dy)) * inv_rho / A;
-      uz = (mz + (C)0.5 * (Gz + Kvz + dz)) * inv_rho / A;
-      Fx = Gx + dx + Kvx - Kp * ux;
-      Fy = Gy + dy + Kvy - Kp * uy;
-      Fz = Gz + dz + Kvz - Kp * uz;
-    }
+    porous_drag<C>(kp, c, eps, rho, inv_rho, A, Kp, Kvx, Kvy, Kvz, Gx, Gy, Gz, mx, my, mz, ux, uy, uz, Fx, Fy,
+                   Fz);
   } else if (pdrag) {
     ux /= A;
     uy /= A;

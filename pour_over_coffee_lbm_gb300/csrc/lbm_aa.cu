@@ -19,7 +19,7 @@
 // the 18 link bits of the cell's own flag word: a cell without any takes the odd step's plain
 // streaming addresses (per-direction offset tables, no per-direction tests), the others choose
 // per direction between the streamed and the bounced slot.
-#include "collide.cuh"
+#include "aa_cell.cuh"
 
 namespace pog {
 
@@ -32,81 +32,6 @@ constexpr int AA_BLOCK = 256;
 #ifndef POG_AA_ONE_CELL
 #define POG_AA_ONE_CELL 1
 #endif
-
-// The 19 incoming populations of cell c as stored values (AA read pattern of PARITY).  Every
-// slot of cell c is element c + (a non-negative offset below 19 n) of the offset tables.  On the
-// odd step, `open` (warp-uniform: no cell of the warp touches a solid neighbour) selects the plain
-// streaming offsets; otherwise each direction chooses its streamed or bounced slot.
-template <int S, int PARITY>
-__device__ __forceinline__ void aa_load(const KParams& kp, const typename Store<S>::E* __restrict__ f,
-                                        uint32_t c, uint32_t fl, bool open, typename Store<S>::E raw[19]) {
-  if (PARITY == 0) {
-#pragma unroll
-    for (int q = 0; q < 19; ++q) raw[q] = f[(uint32_t)q * kp.n + c];
-  } else if (open) {
-#pragma unroll
-    for (int q = 0; q < 19; ++q) raw[q] = f[c + kp.rd[q]];
-  } else {
-    // source c - e_q is the neighbour in direction opp(q); a solid one bounces f_q back
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
-      raw[q] = f[c + (wall ? kp.pl[q] : kp.rd[q])];
-    }
-  }
-}
-
-// Collision of cell c (populations fv in the storage's collision form), its macroscopic outputs
-// and sums, and the AA stores of the post-collision populations (MACRO_ONLY: outputs only).
-template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
-__device__ __forceinline__ void aa_update(const KParams& kp, typename Store<S>::E* __restrict__ f,
-                                          uint32_t c, uint32_t fl, bool open, typename Store<S>::C fv[19],
-                                          const float* __restrict__ force, const float* __restrict__ pdrag,
-                                          const float* __restrict__ eps, const float* __restrict__ u_prev,
-                                          float* __restrict__ u_next, float* __restrict__ rho_out,
-                                          float* __restrict__ u_out, RedAcc<typename Store<S>::C>& acc) {
-  using St = Store<S>;
-  using C = typename St::C;
-  const uint32_t n = kp.n;
-  C nu_st = (C)0;
-  if (!MACRO_ONLY && kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS))
-    nu_st = les_nu_stencil<C>(kp, c, u_prev);
-  const C rs = (C)kp.rho0;  // shift density of the shifted storages
-  const CellResult<C> r =
-      collide_cell<C, St::SHIFTED>(kp, fl, c, fv, force, pdrag, eps, nu_st, (C)St::SCALE, rs);
-  if (rho_out) rho_out[c] = (float)r.rho;
-  if (u_out) {
-    u_out[c] = (float)r.ux;
-    u_out[n + c] = (float)r.uy;
-    u_out[2u * n + c] = (float)r.uz;
-  }
-  if (!MACRO_ONLY && u_next) {
-    u_next[c] = (float)r.ux;
-    u_next[n + c] = (float)r.uy;
-    u_next[2u * n + c] = (float)r.uz;
-  }
-  if (REDUCE) acc.add(r);
-  if (MACRO_ONLY) return;
-  if (PARITY == 0) {
-#pragma unroll
-    for (int q = 0; q < 19; ++q) f[(uint32_t)opp(q) * n + c] = St::ench(fv[q]);
-    return;
-  }
-  if (open) {
-#pragma unroll
-    for (int q = 0; q < 19; ++q) f[c + kp.wr[q]] = St::ench(fv[q]);
-  } else {
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
-      f[c + (wall ? kp.pl[opp(q)] : kp.wr[q])] = St::ench(fv[q]);
-    }
-  }
-}
-
-__device__ __forceinline__ bool aa_live(const KParams& kp, uint32_t c, uint32_t fl) {
-  return !(fl & POG_CELL_SOLID) && c >= kp.guard_lo && c <= kp.guard_hi;
-}
 
 // One cell per thread (grid-stride when the grid is smaller than the lattice).
 template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
@@ -257,6 +182,10 @@ int launch_rows_step(const KParams& kp, int parity, bool reduce, void* f, const 
                      const float* u_prev, float* u_next, float* rho_out, float* u_out, double* red,
                      cudaStream_t s);
 
+int launch_pair_step(const KParams& kp, int parity, bool reduce, void* f, const uint32_t* flags,
+                     const float* force, const float* pdrag, const float* eps, float* rho_out, float* u_out,
+                     double* red, cudaStream_t s);
+
 static int grid_for(uint32_t n, int block) {
   long long want = ((long long)n + block - 1) / block;
   return (int)(want < 152 * 64 ? want : 152 * 64);
@@ -323,6 +252,9 @@ int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, i
     if (p->wall_cells)
       rc = launch_rows_step(kp, parity, reductions != nullptr, f, flags, p->wall_cells, p->n_wall_cells, force,
                             pdrag, porosity, stencil ? up : nullptr, stencil ? un : nullptr,
+                            last ? rho_out : nullptr, last ? u_out : nullptr, reductions, s);
+    else if (p->step_kernel == POG_STEP_AUTO)
+      rc = launch_pair_step(kp, parity, reductions != nullptr, f, flags, force, pdrag, porosity,
                             last ? rho_out : nullptr, last ? u_out : nullptr, reductions, s);
     if (rc == 1)
       rc = dispatch_storage(kp, parity, reductions != nullptr, false, f, flags, force, pdrag, porosity,

@@ -16,6 +16,7 @@ LES_OFF, LES_STENCIL, LES_LOCAL = 0, 1, 2
 DRAG_SEMI_IMPLICIT, DRAG_EXPLICIT_CAP = 0, 1
 REACTION_IMPLICIT, REACTION_EXPLICIT, REACTION_EXPLICIT_NEW = 0, 1, 2
 FORCING_GUO, FORCING_REFERENCE = 0, 1
+STEP_AUTO, STEP_CELLS = 0, 1
 INLET_NCOEF = 16
 
 CELL_SOLID, CELL_INLET, CELL_OUTLET, CELL_POROUS, CELL_NEAR_SOLID = 0x01, 0x02, 0x04, 0x08, 0x10
@@ -47,6 +48,7 @@ class PogParams(ctypes.Structure):
         ("phase", ctypes.c_void_p), ("tau_air", ctypes.c_float),
         ("deposit_mask", ctypes.c_void_p),
         ("wall_cells", ctypes.c_void_p), ("n_wall_cells", ctypes.c_int32),
+        ("step_kernel", ctypes.c_int32),
     ]
 
 

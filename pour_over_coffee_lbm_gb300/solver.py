@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .params import (CELL_INLET, CELL_NEAR_SOLID, CELL_OUTLET, CELL_POROUS, CELL_SOLID,
+from .params import (CELL_INLET, CELL_NEAR_SOLID, CELL_OUTLET, CELL_POROUS, CELL_SOLID, STEP_AUTO, STEP_CELLS,
                      LES_LOCAL, LES_OFF, LES_STENCIL, RED_COUNT, STORE_BF16S, STORE_F16S, STORE_F32, STORE_F64,
                      LatticeConfig)
 
@@ -126,7 +126,7 @@ class GB300LBMSolver:
 
     def __init__(self, config: Optional[LatticeConfig] = None, device: str = "cuda",
                  porosity: Optional[np.ndarray] = None, preferred_backend: Optional[str] = None,
-                 step_kernel: str = "registers"):
+                 step_kernel: str = "auto"):
         if not torch.cuda.is_available():
             raise RuntimeError("GB300LBMSolver needs a CUDA device (no CPU path exists)")
         self.lib = _lib.load()
@@ -143,12 +143,14 @@ class GB300LBMSolver:
         # one 32-bit word per cell: flag bits + bit (8+q) when neighbour q is solid
         self._flags = torch.empty(shape, dtype=torch.int32, device=dev)
         self._build_flags()
-        # "registers" (default, measured faster on GB300): the register-staged step; "rows": the
-        # row-tiled TMA-staged step (with its bounce-back cell list) where it applies.  Same update
-        # either way.
-        if step_kernel not in ("rows", "registers"):
-            raise ValueError("step_kernel must be 'rows' or 'registers'")
+        # "auto" (default): the two-cell step kernel for FP16S/BF16S storage where it applies,
+        # else the per-cell register-staged kernel; "registers": the per-cell kernel for every
+        # storage; "rows": the row-tiled TMA-staged step (with its bounce-back cell list) where it
+        # applies.  Same update in each.
+        if step_kernel not in ("auto", "rows", "registers"):
+            raise ValueError("step_kernel must be 'auto', 'rows' or 'registers'")
         self.step_kernel = step_kernel
+        self._p.step_kernel = STEP_CELLS if step_kernel == "registers" else STEP_AUTO
         self._walls = None
         self._build_wall_list()
         self._f = torch.empty((19,) + shape, dtype=_STORAGE_DTYPE[c.storage], device=dev)
@@ -617,7 +619,7 @@ class GB300LBMSolver:
         self.cfg = self.cfg.replace(les_mode=mode, cs_smag=float(smagorinsky_constant))
         p = self.cfg.to_c()
         for name in ("inlet_control", "pour_control", "filter_blockage", "phase", "deposit_mask",
-                     "wall_cells", "n_wall_cells", "tau_air"):
+                     "wall_cells", "n_wall_cells", "step_kernel", "tau_air"):
             setattr(p, name, getattr(self._p, name))
         self._p = p
         self.use_les = True

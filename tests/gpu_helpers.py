@@ -6,7 +6,7 @@ import numpy as np
 import torch
 
 from pour_over_coffee_lbm_gb300 import _lib
-from pour_over_coffee_lbm_gb300.params import (LES_STENCIL, RED_COUNT, STORE_BF16S, STORE_F16S,
+from pour_over_coffee_lbm_gb300.params import (LES_STENCIL, RED_COUNT, STEP_CELLS, STORE_BF16S, STORE_F16S,
                                                STORE_F32, STORE_F64)
 
 DT = {STORE_F32: torch.float32, STORE_F16S: torch.float16, STORE_BF16S: torch.bfloat16,
@@ -53,9 +53,11 @@ def wall_list(p, flags):
 class AARun:
     """AA-pattern state driven through pog_step."""
 
-    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None, rows=False):
+    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None, rows=False, cells=False):
         self.cfg = cfg
         self.p = cfg.to_c()
+        if cells:
+            self.p.step_kernel = STEP_CELLS  # the per-cell kernel even where the two-cell one applies
         shape = (cfg.nz, cfg.ny, cfg.nx)
         self.flags = gpu_flags(cfg) if flags is None else torch.as_tensor(np.asarray(flags).astype(np.int32)).cuda()
         self.walls = None
@@ -95,8 +97,8 @@ class AARun:
         return nat.cpu().numpy()
 
 
-def run_aa(cfg, steps, eps=None, force=None, reduce=True, pdrag=None, rows=False):
-    r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows)
+def run_aa(cfg, steps, eps=None, force=None, reduce=True, pdrag=None, rows=False, cells=False):
+    r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows, cells=cells)
     if steps > 1:
         r.step(steps - 1, reduce=reduce, macro=False)
     r.step(1, reduce=reduce, macro=True)
