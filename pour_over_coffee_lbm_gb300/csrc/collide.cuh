@@ -114,12 +114,32 @@ __host__ __device__ __forceinline__ PairCoef<C> pair_coef(C a1, C b3, C uF, C ba
   k.b3 = b3;
   return k;
 }
+// e_q . v with only the non-zero components of e_q (signs folded at compile time).  Same value
+// as cx v_x + cy v_y + cz v_z summed left to right: the zero terms add nothing, and IEEE
+// arithmetic would not let the compiler drop 0 * v itself.
+template <int Q, typename C>
+__host__ __device__ __forceinline__ C edotq(C x, C y, C z) {
+  constexpr int a = cx(Q), b = cy(Q), c = cz(Q);
+  C r;
+  if constexpr (a != 0) {
+    r = a > 0 ? x : -x;
+    if constexpr (b != 0) r = b > 0 ? r + y : r - y;
+    if constexpr (c != 0) r = c > 0 ? r + z : r - z;
+  } else if constexpr (b != 0) {
+    r = b > 0 ? y : -y;
+    if constexpr (c != 0) r = c > 0 ? r + z : r - z;
+  } else {
+    r = c > 0 ? z : -z;
+  }
+  return r;
+}
+
 template <int Q, typename C>
 __host__ __device__ __forceinline__ void collide_pair(C f[19], C ux, C uy, C uz, C Fx, C Fy, C Fz, C keep,
                                                       const PairCoef<C>& k) {
   constexpr int P = opp(Q);
-  const C eu = (C)cx(Q) * ux + (C)cy(Q) * uy + (C)cz(Q) * uz;
-  const C eF = (C)cx(Q) * Fx + (C)cy(Q) * Fy + (C)cz(Q) * Fz;
+  const C eu = edotq<Q, C>(ux, uy, uz);
+  const C eF = edotq<Q, C>(Fx, Fy, Fz);
   const C sym = fma(eu, fma(k.Cc, eF, k.B * eu), k.A);
   const C asym = fma(k.D, eu, k.b3 * eF);
   const C fq = f[Q], fp = f[P];
@@ -135,10 +155,8 @@ __device__ __forceinline__ void collide_pair2(C f[19], C ux, C uy, C uz, C Fx, C
                                               const PairCoef<C>& k) {
   static_assert(sizeof(C) == 4, "packed pairs are FP32");
   constexpr int P1 = opp(Q1), P2 = opp(Q2);
-  const float2 EU = make_float2((C)cx(Q1) * ux + (C)cy(Q1) * uy + (C)cz(Q1) * uz,
-                                (C)cx(Q2) * ux + (C)cy(Q2) * uy + (C)cz(Q2) * uz);
-  const float2 EF = make_float2((C)cx(Q1) * Fx + (C)cy(Q1) * Fy + (C)cz(Q1) * Fz,
-                                (C)cx(Q2) * Fx + (C)cy(Q2) * Fy + (C)cz(Q2) * Fz);
+  const float2 EU = make_float2(edotq<Q1, C>(ux, uy, uz), edotq<Q2, C>(ux, uy, uz));
+  const float2 EF = make_float2(edotq<Q1, C>(Fx, Fy, Fz), edotq<Q2, C>(Fx, Fy, Fz));
   const float2 A = make_float2(k.A, k.A), B = make_float2(k.B, k.B), Cc = make_float2(k.Cc, k.Cc);
   const float2 D = make_float2(k.D, k.D), b3 = make_float2(k.b3, k.b3), K = make_float2(keep, keep);
   const float2 sym = __ffma2_rn(EU, __ffma2_rn(Cc, EF, __fmul2_rn(B, EU)), A);

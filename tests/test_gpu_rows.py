@@ -1,5 +1,5 @@
 """GPU parity of the row-tiled step kernel (csrc/lbm_tma.cu) against the register-staged step
-kernel (csrc/lbm_aa.cu), both through pog_step.
+kernel (csrc/lbm_aa.cu, selected with POG_STEP_CELLS), both through pog_step.
 
 Both kernels run the same per-cell collision code on the same incoming populations, so the bar is
 bit equality: the whole distribution state, and the rho / u outputs, after even and odd step
@@ -26,7 +26,7 @@ def _pair(cfg, steps, eps=None, force=None, pdrag=None, reduce=True):
     """Run the same case with both kernels; return the two AARun objects."""
     out = []
     for rows in (False, True):
-        r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows)
+        r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows, cells=not rows)
         if steps > 1:
             r.step(steps - 1, reduce=reduce, macro=False)
         r.step(1, reduce=reduce, macro=True)
@@ -111,7 +111,7 @@ def test_rows_kernel_with_every_step_input(cuda, orc):
     mask = torch.as_tensor(words.view(np.int32)).cuda()
     runs = []
     for rows in (False, True):
-        r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows)
+        r = AARun(cfg, eps=eps, force=force, pdrag=pdrag, rows=rows, cells=not rows)
         r.p.deposit_mask = P(mask)
         r.step(24, reduce=True, macro=False)
         r.step(1, reduce=True, macro=True)
@@ -125,8 +125,8 @@ def test_rows_kernel_with_every_step_input(cuda, orc):
 def test_kernels_mix_step_by_step(cuda):
     """Between steps both kernels leave the same state: alternating them changes nothing."""
     cfg = LatticeConfig(nx=64, ny=64, nz=64, les_mode=LES_LOCAL, band_thickness=3.0, storage=STORE_F16S)
-    ref = AARun(cfg)
-    mix = AARun(cfg, rows=True)
+    ref = AARun(cfg, cells=True)
+    mix = AARun(cfg, rows=True, cells=True)
     walls = mix.p.wall_cells
     for t in range(30):
         ref.step(1, macro=False)
