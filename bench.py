@@ -419,8 +419,9 @@ def differentiation_rows(peak):
         hh = (ep[c].double() - em[c].double()).item() / 2
         fd = (run.loss_frozen(ep.reshape(eps.shape), coef) - run.loss_frozen(em.reshape(eps.shape), coef)) / (2 * hh)
         err_eps = max(err_eps, abs(ge[c] - fd) / max(abs(fd), 1e-30))
+    err_eps = float(err_eps)
     out["fd_fp64_h1e-3"] = {"inlet_16_vs_largest": err_in, "porosity_8_max_rel": err_eps,
-                            "bar": 1e-4, "ok": err_in <= 1e-4 and err_eps <= 1e-4,
+                            "bar": 1e-4, "ok": bool(err_in <= 1e-4 and err_eps <= 1e-4),
                             "inlet_fd_recorded_forcing": fds.tolist(), "inlet_adjoint": ads.tolist(),
                             "inlet_fd_particles_responding": fdc.tolist(),
                             "particle_feedback_vs_largest": float(np.max(np.abs(fdc - fds)) / np.max(np.abs(fds)))}

@@ -59,7 +59,7 @@ enum pog_storage {     /* how the distributions are stored in HBM               
   POG_STORE_F32 = 0,   /* float (f_i - w_i*rho0); collision in FP32 on the deviations        */
   POG_STORE_F16S = 1,  /* IEEE half of (f_i - w_i*rho0)*2^12; collision in FP32              */
   POG_STORE_BF16S = 2, /* bfloat16 of (f_i - w_i*rho0); collision in FP32                    */
-  POG_STORE_F64 = 3    /* double f_i, collision in FP64 (reference runs for error reports)  */
+  POG_STORE_F64 = 3    /* double (f_i - w_i*rho0); collision in FP64 (reference runs)       */
 };
 /* The stored form is internal: pog_export_natural / pog_import_natural convert to and from
  * plain f_i in FP32 or FP64 for every storage. */
@@ -395,8 +395,10 @@ int pog_wall_list(const pog_params* p, const uint32_t* flags, int32_t* cells, in
                   int32_t* count, void* stream);
 
 /* Same step on the natural (two-buffer) layout: reads f_in at time t, writes f_out at t+1
- * with push streaming exactly as legacy/lbm_solver.py:609-628.  Used for checkpointed
- * recomputation under the adjoint and for FP64 reference runs. */
+ * with push streaming exactly as legacy/lbm_solver.py:609-628.  Both buffers hold slot (q, c) in
+ * p->storage's stored form (the shifted deviation of enum pog_storage), which is also the AA
+ * state at an even t: pog_import_natural fills f_in, pog_export_natural (t even) reads f_out.
+ * Used for checkpointed recomputation under the adjoint and for FP64 reference runs. */
 int pog_step_push(const pog_params* p, const void* f_in, void* f_out, const uint32_t* flags,
                   const float* force, const float* pdrag, const float* porosity, const float* u_prev,
                   float* rho_out, float* u_out, double* reductions, void* stream);
@@ -501,9 +503,11 @@ size_t pog_adjoint_scratch_bytes(const pog_params* p);
 
 /* The outflow flux of a natural-layout state f_nat (F32 or F64 storage), flux = -sum over outlet
  * cells of sum_q c_qz f_q -- the POG_RED_OUTFLOW contribution of the step that starts from f_nat --
- * added to *acc (DEVICE int64) in fixed point, units of 2^-48.  Integer sums do not depend on the
- * order of accumulation, so a loss J = sum_t flux_t built from it is the same bits on every run
- * (finite differences of J then carry no reduction-order noise). */
+ * added to acc[0..1] (DEVICE int64 x 2) in two-word fixed point: acc[0] in units of 2^-48 (each
+ * cell's flux rounded), acc[1] the cells' rounding remainders in units of 2^-96, so
+ * acc[0] 2^-48 + acc[1] 2^-96 is the exact sum of the cells' FP64 fluxes.  Integer sums do not
+ * depend on the order of accumulation, so a loss J = sum_t flux_t built from it is the same bits
+ * on every run, and finite differences of J carry neither reduction-order nor quantisation noise. */
 int pog_outflow_fixed(const pog_params* p, const void* f_nat, const uint32_t* flags, long long* acc,
                       void* stream);
 

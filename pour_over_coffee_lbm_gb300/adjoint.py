@@ -63,8 +63,8 @@ class OutflowAdjoint:
                       for _ in range(self.nseg)]
         self._states = [torch.empty((19,) + shape, dtype=self.dtype, device=self.device)
                         for _ in range(self.K)]
-        # J in fixed point (units of 2^-48): the same bits on every run
-        self._jfix = torch.zeros(1, dtype=torch.int64, device=self.device)
+        # J in two-word fixed point (units of 2^-48 and 2^-96): the exact sum, the same bits on every run
+        self._jfix = torch.zeros(2, dtype=torch.int64, device=self.device)
         self._p = None
         self._eps = None
         self.pc = particles
@@ -197,7 +197,8 @@ class OutflowAdjoint:
         return self._loss()
 
     def _loss(self) -> float:
-        return float(self._jfix.item()) * 2.0 ** -48
+        hi, lo = (int(v) for v in self._jfix.tolist())
+        return float(hi) * 2.0 ** -48 + float(lo) * 2.0 ** -96
 
     def backward(self, want_porosity_grad: bool = True) -> AdjointResult:
         s = _lib.stream_handle()

@@ -548,13 +548,17 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
 // not depend on the order in which blocks arrive and repeated runs agree bit for bit.
 constexpr double OUTFLOW_FIX_SCALE = 281474976710656.0;  // 2^48
 
+// acc[0] += the flux in units of 2^-48 (rounded per cell), acc[1] += each cell's rounding remainder
+// in units of 2^-96.  x 2^48 is exact (a power of two), the remainder xs - rint(xs) is exact
+// (|xs - rint(xs)| <= 1/2 and Sterbenz), and so is its scaling by 2^48: the two words hold the
+// exact sum of the per-cell FP64 fluxes down to 2^-96, in integers, whatever the order.
 template <int S>
 __global__ void outflow_fixed_kernel(const KParams kp, const typename Store<S>::E* __restrict__ f,
                                      const uint32_t* __restrict__ flags, unsigned long long* __restrict__ acc) {
   using St = Store<S>;
   using C = typename St::C;
   const uint32_t n = kp.n;
-  long long part = 0;
+  long long hi = 0, lo = 0;
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
     const uint32_t fl = flags[c];
     if (!(fl & POG_CELL_OUTLET) || (fl & POG_CELL_SOLID)) continue;
@@ -562,9 +566,13 @@ __global__ void outflow_fixed_kernel(const KParams kp, const typename Store<S>::
 #pragma unroll
     for (int q = 0; q < 19; ++q)
       if (cz(q) != 0) mz += (C)cz(q) * St::ld(f, (uint32_t)q * n + c, q, (C)kp.rho0);
-    part += __double2ll_rn(-(double)mz * OUTFLOW_FIX_SCALE);
+    const double xs = -(double)mz * OUTFLOW_FIX_SCALE;
+    const double r = rint(xs);
+    hi += (long long)r;
+    lo += __double2ll_rn((xs - r) * OUTFLOW_FIX_SCALE);
   }
-  if (part != 0) atomicAdd(acc, (unsigned long long)part);
+  if (hi != 0) atomicAdd(acc, (unsigned long long)hi);
+  if (lo != 0) atomicAdd(acc + 1, (unsigned long long)lo);
 }
 
 }  // namespace pog

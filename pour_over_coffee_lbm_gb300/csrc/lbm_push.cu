@@ -23,13 +23,16 @@ __global__ void __launch_bounds__(PUSH_BLOCK, S == POG_STORE_F64 ? 1 : 4) push_s
     const uint32_t fl = flags[c];
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
     const C rs = (C)kp.rho0;  // shift density of the shifted storages
+    // the stored form is collided directly (the deviations h of the shifted storages; the shift
+    // and bounce-back commute: slots q and opp q carry the same weight)
     C fv[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) fv[q] = St::ld(fin, (uint32_t)q * n + c, q, rs);
+    for (int q = 0; q < 19; ++q) fv[q] = St::dech(fin[(uint32_t)q * n + c]);
     C nu_st = (C)0;
     if (kp.les_mode == POG_LES_STENCIL && u_prev && !(fl & POG_CELL_POROUS))
       nu_st = les_nu_stencil<C>(kp, c, u_prev);
-    const CellResult<C> r = collide_cell<C>(kp, fl, c, fv, force, pdrag, eps, nu_st);
+    const CellResult<C> r =
+        collide_cell<C, St::SHIFTED>(kp, fl, c, fv, force, pdrag, eps, nu_st, (C)St::SCALE, rs);
     if (rho_out) rho_out[c] = (float)r.rho;
     if (u_out) {
       u_out[c] = (float)r.ux;
@@ -44,9 +47,9 @@ __global__ void __launch_bounds__(PUSH_BLOCK, S == POG_STORE_F64 ? 1 : 4) push_s
       const uint32_t dst = c + (uint32_t)kp.off[q];
       const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
       if (wall)
-        St::st(fout, (uint32_t)opp(q) * n + c, q, fv[q], rs);
+        fout[(uint32_t)opp(q) * n + c] = St::ench(fv[q]);
       else
-        St::st(fout, (uint32_t)q * n + dst, q, fv[q], rs);
+        fout[(uint32_t)q * n + dst] = St::ench(fv[q]);
     }
   }
   if (REDUCE) reduce_add<C>(acc, red);

@@ -110,7 +110,10 @@ def test_aa_equals_push_f64(cuda):
     f, rho, u, red, fl = run_push(cfg, steps)
     fluid = (fl.cpu().numpy() & CELL_SOLID) == 0
     nat = r.natural()
-    assert rel_l2(nat[:, fluid], f.cpu().numpy()[:, fluid]) < 1e-13
+    # the push buffers hold the shifted form f - w_q rho0 (natural layout)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12).reshape(19, 1, 1, 1)
+    pushed = f.cpu().numpy() + w * cfg.rho0
+    assert rel_l2(nat[:, fluid], pushed[:, fluid]) < 1e-13
     assert np.allclose(r.red.cpu().numpy(), red.cpu().numpy(), rtol=1e-12, atol=1e-14)
 
 
