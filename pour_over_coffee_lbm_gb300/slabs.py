@@ -215,6 +215,15 @@ class RankHalo:
             for r in self.dist.batch_isend_irecv(ops):
                 r.wait()
 
+    def reduce_sums(self, t: torch.Tensor) -> torch.Tensor:
+        """Sum a per-rank tensor over all ranks, in place (all-reduce).  For the step's FP64 sums
+        (POG_RED_*: each rank's pog_step sums only its owned planes, the ghost planes lying
+        outside the step's guard range), the adjoint's inlet-coefficient gradients and, exactly,
+        the integer words of the fixed-point outflow loss.  The per-cell porosity gradient is
+        owned by slab and needs no reduction."""
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return t
+
     def exchange_in(self, f: torch.Tensor):
         below = self.rank - 1 if self.rank > 0 else None
         above = self.rank + 1 if self.rank < self.world - 1 else None

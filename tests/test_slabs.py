@@ -12,6 +12,7 @@ import torch.distributed as dist
 import torch.multiprocessing as mp
 
 import np_aa
+from pour_over_coffee_lbm_gb300.params import RED_COUNT
 from pour_over_coffee_lbm_gb300.slabs import DOWN, UP, RankHalo, slab_bounds, slab_flags, writer_masks
 
 NX, NY, NZ, STEPS, OMEGA = 14, 12, 18, 23, 1.25
@@ -146,15 +147,20 @@ def _rank_oracle(rank, world, port, outdir):
     ft = torch.from_numpy(fs)  # shares memory with fs
     halo = RankHalo(fl, rank, world)
     scfg = cfg.replace(nz=z1 - z0 + 2)
+    red = np.zeros(RED_COUNT)
     for t in range(ORC_STEPS):
         if t % 2:
             halo.exchange_in(ft)
-        oracle.step_aa(scfg, fl, fs, t)
+        oracle.step_aa(scfg, fl, fs, t, reductions=red)
         if t % 2:
             halo.exchange_out(ft)
     if ORC_STEPS % 2:
         halo.exchange_in(ft)
     np.save(os.path.join(outdir, "oslab%d.npy" % rank), fs)
+    # the step sums of the owned planes, and an integer count, summed over the ranks
+    tot = halo.reduce_sums(torch.from_numpy(red))
+    cnt = halo.reduce_sums(torch.tensor([int(((fl[1:-1] & 1) == 0).sum())], dtype=torch.int64))
+    np.save(os.path.join(outdir, "ored%d.npy" % rank), np.concatenate([tot.numpy(), cnt.numpy().astype(np.float64)]))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -186,6 +192,15 @@ def test_rank_halo_with_the_oracle_aa_step(tmp_path, world):
         got[:, z0:z1] = _natural(fs, slab_flags(flags, z0, z1), ORC_STEPS)[:, 1:-1]
     assert np.array_equal(got[:, live], ref[:, live])
     assert np.abs(ref[:, live] - f0[:, live]).max() > 1e-4  # the state did evolve
+    # all-reduced step sums: the undivided run's, up to the order of the FP64 additions
+    red = np.zeros(RED_COUNT)
+    aa = f0.copy()
+    for t in range(ORC_STEPS):
+        oracle.step_aa(cfg, flags, aa, t, reductions=red)
+    for r in range(world):
+        got_red = np.load(tmp_path / ("ored%d.npy" % r))
+        assert np.allclose(got_red[:RED_COUNT], red, rtol=1e-12, atol=1e-12 * abs(red[0])), (got_red, red)
+        assert got_red[RED_COUNT] == int(((flags[:, :, :] & 1) == 0).sum())
 
 
 # ---- slab-owned particles (RankParticles) with the oracle's coupling pass and AA step --------------
