@@ -23,19 +23,24 @@
 
 namespace pog {
 
-constexpr int AA_BLOCK = 256;
-// Resident-block hint for the step kernel (caps registers per thread) and whether the non-
-// reducing variants run one cell per thread (1) or a persistent grid-stride loop (0).
-#ifndef POG_AA_MINB
-#define POG_AA_MINB 4
-#endif
+constexpr int AA_BLOCK = 128;
+// Resident 128-thread blocks per SM the step kernel is compiled for (it caps the registers per
+// thread): 9 (56 registers, 36 warps per SM) for the plain FP32/16-bit step, 8 (64) for the
+// variants with the FP64 sums, 3 (168) for FP64 storage -- each the most that compiles without
+// spilling.  At 256^3 the 56-register step runs 40.3 GLUPS FP32 against 37.9 with 256-thread
+// blocks at 64 registers (32 warps).
+template <int S, bool REDUCE>
+constexpr int aa_min_blocks() {
+  return S == POG_STORE_F64 ? 3 : (REDUCE ? 8 : 9);
+}
+// Whether the non-reducing variants run one cell per thread (1) or a persistent grid-stride loop (0).
 #ifndef POG_AA_ONE_CELL
 #define POG_AA_ONE_CELL 1
 #endif
 
 // One cell per thread (grid-stride when the grid is smaller than the lattice).
 template <int S, int PARITY, bool REDUCE, bool MACRO_ONLY>
-__global__ void __launch_bounds__(AA_BLOCK, POG_AA_MINB) aa_step_kernel(
+__global__ void __launch_bounds__(AA_BLOCK, (aa_min_blocks<S, REDUCE>())) aa_step_kernel(
     const KParams kp, typename Store<S>::E* __restrict__ f, const uint32_t* __restrict__ flags,
     const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
     const float* __restrict__ u_prev, float* __restrict__ u_next, float* __restrict__ rho_out,

@@ -30,10 +30,13 @@
 
 namespace pog {
 
-constexpr int PAIR_BLOCK = 256;
-#ifndef POG_PAIR_MINB
-#define POG_PAIR_MINB 3
-#endif
+constexpr int PAIR_BLOCK = 128;
+// Resident 128-thread blocks per SM: 7 (72 registers, a few spilled bytes; 54.1 GLUPS FP16S at
+// 256^3 against 53.0 at 80 registers) for the plain step, 6 (80) with the FP64 sums.
+template <bool REDUCE>
+constexpr int pair_min_blocks() {
+  return REDUCE ? 6 : 7;
+}
 
 using F2 = float2;  // .x = cell c0, .y = cell c0 + 1
 __device__ __forceinline__ F2 sp2(float a) { return make_float2(a, a); }
@@ -120,7 +123,7 @@ __device__ __forceinline__ void collide_dir2(uint32_t w[19], F2 ux, F2 uy, F2 uz
 }
 
 template <int S, bool REDUCE>
-__global__ void __launch_bounds__(PAIR_BLOCK, POG_PAIR_MINB) aa_pair_even_kernel(
+__global__ void __launch_bounds__(PAIR_BLOCK, (pair_min_blocks<REDUCE>())) aa_pair_even_kernel(
     const KParams kp, typename Store<S>::E* __restrict__ f, const uint32_t* __restrict__ flags,
     const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
     float* __restrict__ rho_out, float* __restrict__ u_out, double* __restrict__ red) {
