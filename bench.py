@@ -556,11 +556,11 @@ def precision_cfg(storage, case):
                          band=kw.get("band", 3.0))
 
 
-def precision_line(storage, steps, peak, case="les_band", step_kernel="auto"):
+def precision_line(storage, steps, peak, case="les_band", step_kernel="auto", density_reference=False):
     import torch
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     cfg = precision_cfg(storage, case)
-    s = GB300LBMSolver(cfg, step_kernel=step_kernel)
+    s = GB300LBMSolver(cfg, step_kernel=step_kernel, density_reference=density_reference)
     for _ in range(4):
         s.run(1)
     torch.cuda.synchronize()
@@ -600,8 +600,8 @@ def precision_errors(steps, case="les_band"):
     from pour_over_coffee_lbm_gb300.solver import GB300LBMSolver
     checks = sorted({c for c in (500, 1000, steps) if c <= steps})
 
-    def trajectory(st):
-        s = GB300LBMSolver(precision_cfg(st, case))
+    def trajectory(st, ref=False):
+        s = GB300LBMSolver(precision_cfg(st, case), density_reference=ref)
         done, out = 0, {}
         for c in checks:
             s.run(c - done - 1)
@@ -615,8 +615,9 @@ def precision_errors(steps, case="les_band"):
 
     ref, fluid = trajectory(STORE_F64)
     res = {"steps": checks}
-    for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
-        got, _ = trajectory(st)
+    for name, st, ref_d in (("fp32", STORE_F32, False), ("fp16s", STORE_F16S, False),
+                            ("fp16s_ref", STORE_F16S, True), ("bf16s", STORE_BF16S, False)):
+        got, _ = trajectory(st, ref_d)
         res[name] = {"u_rel_l2": [], "rho_rel_l2": []}
         for c in checks:
             u, r = got[c]
@@ -894,10 +895,13 @@ def run_ours(args):
             for name, st in (("fp32", STORE_F32), ("fp16s", STORE_F16S), ("bf16s", STORE_BF16S)):
                 kernels = ("rows", "registers") if st == STORE_F32 else ("rows", "registers", "auto")
                 lines[name] = {k: precision_line(st, 200, peak, case, k) for k in kernels}
+            # FP16S stored relative to per-cell reference densities (pog_params.density_ref)
+            lines["fp16s_ref"] = {"auto": precision_line(STORE_F16S, 200, peak, case, "auto", True)}
             best = {n: max(v.values(), key=lambda d: d["mlups"]) for n, v in lines.items()}
             errs = precision_errors(args.error_steps, case) if args.error_steps > 0 else None
             extra[case] = {"workload": label, "lines": lines, "error_vs_fp64": errs,
                            "fp16s_vs_fp32_mlups": round(best["fp16s"]["mlups"] / best["fp32"]["mlups"], 3),
+                           "fp16s_ref_vs_fp32_mlups": round(best["fp16s_ref"]["mlups"] / best["fp32"]["mlups"], 3),
                            "bf16s_vs_fp32_mlups": round(best["bf16s"]["mlups"] / best["fp32"]["mlups"], 3)}
         coupled = coupled_line(args, peak)
         rows = plugin_rows(*workload(False), 200, peak)

@@ -155,6 +155,18 @@ typedef struct pog_params {
    * two-cell kernel's collision rounds differently in FP32, so 16-bit stored values can differ
    * by one unit in their last place. */
   int32_t step_kernel;
+  /* Optional DEVICE array [ncell] of IEEE half values d_c, or NULL (FP16S storage only).  With it,
+   * FP16S stores each slot relative to the reference density rho0 + d_c of the cell that owns
+   * the slot instead of rho0: every even step a cell sets d_c to its density deviation (rounded
+   * to FP16) and re-encodes its populations, every odd step moves the populations it streams
+   * between its neighbours' references and its own.  The stored deviations then carry the
+   * velocity information without the pressure waves' density swing, which FP16's 11-bit
+   * significand otherwise rounds against (u error vs FP64 at 256^3 LES + band, 2,000 steps:
+   * see the design notes).  pog_init_equilibrium sets it; pog_export_natural /
+   * pog_import_natural / pog_macroscopic read it; pog_step_push rejects it; the two-cell and
+   * row-tiled kernels do not run with it.  Keep it with the distributions (checkpoints, halos):
+   * the stored state means nothing without it.  No counterpart in the reference. */
+  void* density_ref;
 } pog_params;
 
 enum pog_step_kernel { POG_STEP_AUTO = 0, POG_STEP_CELLS = 1 };

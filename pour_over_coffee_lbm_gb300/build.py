@@ -23,6 +23,7 @@ SOURCES = {
     "lbm_aa.cu": FAST_F32,
     "lbm_tma.cu": FAST_F32,
     "lbm_pair.cu": FAST_F32,
+    "lbm_ref.cu": FAST_F32,
     "lbm_push.cu": [],
     "particles.cu": ["-fmad=false"],
     "particles_noalloc.cu": [],

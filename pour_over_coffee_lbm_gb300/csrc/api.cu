@@ -85,6 +85,7 @@ KParams make_kparams(const pog_params* p) {
   k.phase = p->phase;
   k.tau_air = p->tau_air;
   k.dmask = p->deposit_mask;
+  k.dref = (__half*)p->density_ref;
   return k;
 }
 
@@ -141,6 +142,8 @@ int pog_validate_params(const pog_params* p) {
     return set_error(POG_E_ARG, "n_wall_cells=%d must be >= 0", p->n_wall_cells);
   if (p->step_kernel != POG_STEP_AUTO && p->step_kernel != POG_STEP_CELLS)
     return set_error(POG_E_ARG, "step_kernel=%d unknown", p->step_kernel);
+  if (p->density_ref && p->storage != POG_STORE_F16S)
+    return set_error(POG_E_ARG, "density_ref needs FP16S storage (storage=%d)", p->storage);
   if (p->clamp_tau && !(p->tau_min > 0.5f && p->tau_max >= p->tau_min))
     return set_error(POG_E_ARG, "tau clamp [%g,%g] invalid", (double)p->tau_min, (double)p->tau_max);
   return POG_OK;

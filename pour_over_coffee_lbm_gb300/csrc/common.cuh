@@ -66,9 +66,19 @@ struct KParams {
   const float* phase;      // device phase indicator [n] (0 air, 1 water) or null
   float tau_air;
   const uint32_t* dmask;   // device bit mask of the cells with a particle deposit, or null
+  __half* dref;            // FP16S per-cell reference density deviations [n], or null
 };
 
 KParams make_kparams(const pog_params* p);
+
+// A copy of a register the compiler cannot see through (so it neither merges two computations
+// of the same value nor keeps the first alive until the second): a kernel recomputes an address
+// or a conversion instead of holding it in a register across the collision.
+__device__ __forceinline__ uint32_t opaque(uint32_t v) {
+  uint32_t r;
+  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+  return r;
+}
 
 // Error plumbing (thread-local message, no exceptions across the ABI).
 int set_error(int code, const char* fmt, ...);

@@ -190,6 +190,14 @@ int launch_rows_step(const KParams& kp, int parity, bool reduce, void* f, const 
 int launch_pair_step(const KParams& kp, int parity, bool reduce, void* f, const uint32_t* flags,
                      const float* force, const float* pdrag, const float* eps, float* rho_out, float* u_out,
                      double* red, cudaStream_t s);
+int launch_ref_step(const KParams& kp, int parity, bool reduce, bool macro, void* f, const uint32_t* flags,
+                    const float* force, const float* pdrag, const float* eps, const float* u_prev, float* u_next,
+                    float* rho_out, float* u_out, double* red, cudaStream_t s);
+int ref_export(const KParams& kp, const void* f, const uint32_t* flags, int parity, void* f_nat, int out_storage,
+               cudaStream_t s);
+int ref_import(const KParams& kp, const void* f_nat, int in_storage, const uint32_t* flags, void* f, cudaStream_t s);
+int ref_init(const KParams& kp, void* f, const uint32_t* flags, float rho, float ux, float uy, float uz,
+             cudaStream_t s);
 
 static int grid_for(uint32_t n, int block) {
   long long want = ((long long)n + block - 1) / block;
@@ -220,6 +228,7 @@ int pog_init_equilibrium(const pog_params* p, void* f, const uint32_t* flags, fl
   if (!f || !flags) return set_error(POG_E_ARG, "f/flags is NULL");
   KParams kp = make_kparams(p);
   cudaStream_t s = (cudaStream_t)stream;
+  if (kp.dref) return ref_init(kp, f, flags, rho0, ux, uy, uz, s);
   int g = grid_for(kp.n, 256);
   switch (p->storage) {
     case POG_STORE_F32: aa_init_kernel<POG_STORE_F32><<<g, 256, 0, s>>>(kp, (float*)f, flags, rho0, ux, uy, uz); break;
@@ -254,7 +263,11 @@ int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, i
     const int parity = (int)((t + i) & 1);
     // the row-tiled kernel when the caller supplied the bounce-back cell list (and it applies)
     rc = 1;
-    if (p->wall_cells)
+    if (kp.dref)
+      rc = launch_ref_step(kp, parity, reductions != nullptr, false, f, flags, force, pdrag, porosity,
+                           stencil ? up : nullptr, stencil ? un : nullptr, last ? rho_out : nullptr,
+                           last ? u_out : nullptr, reductions, s);
+    else if (p->wall_cells)
       rc = launch_rows_step(kp, parity, reductions != nullptr, f, flags, p->wall_cells, p->n_wall_cells, force,
                             pdrag, porosity, stencil ? up : nullptr, stencil ? un : nullptr,
                             last ? rho_out : nullptr, last ? u_out : nullptr, reductions, s);
@@ -283,6 +296,9 @@ int pog_macroscopic(const pog_params* p, const void* f, const uint32_t* flags, l
   if (!f || !flags) return set_error(POG_E_ARG, "f/flags is NULL");
   KParams kp = make_kparams(p);
   if (kp.les_mode == POG_LES_STENCIL) kp.les_mode = POG_LES_OFF;  // u does not depend on tau
+  if (kp.dref)
+    return launch_ref_step(kp, (int)(t & 1), false, true, (void*)f, flags, force, pdrag, nullptr, nullptr, nullptr,
+                           rho_out, u_out, nullptr, (cudaStream_t)stream);
   return dispatch_storage(kp, (int)(t & 1), false, true, (void*)f, flags, force, pdrag, nullptr, nullptr,
                           nullptr, rho_out, u_out, nullptr, (cudaStream_t)stream);
 }
@@ -296,8 +312,9 @@ int pog_export_natural(const pog_params* p, const void* f, const uint32_t* flags
     return set_error(POG_E_ARG, "out_storage must be F32 or F64");
   KParams kp = make_kparams(p);
   cudaStream_t s = (cudaStream_t)stream;
-  int g = grid_for(kp.n, 256);
   const int par = (int)(t & 1);
+  if (kp.dref) return ref_export(kp, f, flags, par, f_nat, out_storage, s);
+  int g = grid_for(kp.n, 256);
 #define POG_EXP(SS, E)                                                                         \
   if (p->storage == SS) {                                                                      \
     if (out_storage == POG_STORE_F32) {                                                        \
@@ -327,6 +344,7 @@ int pog_import_natural(const pog_params* p, const void* f_nat, int in_storage, c
     return set_error(POG_E_ARG, "in_storage must be F32 or F64");
   KParams kp = make_kparams(p);
   cudaStream_t s = (cudaStream_t)stream;
+  if (kp.dref) return ref_import(kp, f_nat, in_storage, flags, f, s);
   int g = grid_for(kp.n, 256);
 #define POG_IMP(SS, E)                                                                          \
   if (p->storage == SS) {                                                                       \

@@ -44,14 +44,6 @@ __device__ __forceinline__ F2 add2(F2 a, F2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ F2 sub2(F2 a, F2 b) { return __ffma2_rn(b, sp2(-1.0f), a); }  // a - b, one rounding
 __device__ __forceinline__ F2 mul2(F2 a, F2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) { return __ffma2_rn(a, b, c); }
-// A copy of a register the compiler cannot see through: the collision converts a population
-// pair again from its packed word instead of keeping the moment pass's two floats alive
-// (19 registers, not 38).
-__device__ __forceinline__ uint32_t opaque(uint32_t v) {
-  uint32_t r;
-  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
-  return r;
-}
 
 // Packed 16-bit pair <-> two floats (low half = the even cell).
 template <int S>
@@ -117,6 +109,8 @@ __device__ __forceinline__ void collide_dir2(uint32_t w[19], F2 ux, F2 uy, F2 uz
   const F2 eu = edot<Q>(ux, uy, uz), eF = edot<Q>(Fx, Fy, Fz);
   const F2 sym = fma2(eu, fma2(k.Cc, eF, mul2(k.B, eu)), k.A);
   const F2 asym = fma2(k.D, eu, mul2(k.b3, eF));
+  // converted again from the packed words (opaque copies), not kept from the moment pass: 19
+  // registers instead of 38
   const F2 hq = Pair16<S>::unpack(opaque(w[Q])), hp = Pair16<S>::unpack(opaque(w[P]));
   w[Q] = Pair16<S>::pack(fma2(keep, hq, add2(sym, asym)));
   w[P] = Pair16<S>::pack(fma2(keep, hp, sub2(sym, asym)));
@@ -364,6 +358,7 @@ int launch_pair_step(const KParams& kp, int parity, bool reduce, void* f, const 
                      double* red, cudaStream_t s) {
   if (parity != 0) return 1;
   if (kp.storage != POG_STORE_F16S && kp.storage != POG_STORE_BF16S) return 1;
+  if (kp.dref) return 1;  // the per-cell reference form runs in lbm_ref.cu
   if ((kp.nx & 1u) || kp.les_mode == POG_LES_STENCIL || kp.forcing_mode != POG_FORCING_GUO || kp.phase) return 1;
   if (!aligned(f, 4) || !aligned(flags, 8) || !aligned(force, 8) || !aligned(rho_out, 8) || !aligned(u_out, 8))
     return 1;

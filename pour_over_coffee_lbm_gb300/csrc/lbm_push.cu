@@ -6,10 +6,16 @@
 
 namespace pog {
 
-constexpr int PUSH_BLOCK = 256;
+constexpr int PUSH_BLOCK = 128;
+// Resident 128-thread blocks per SM, as the AA step: 9 (56 registers), 8 with the FP64 sums, 3
+// for FP64 storage.
+template <int S, bool REDUCE>
+constexpr int push_min_blocks() {
+  return S == POG_STORE_F64 ? 3 : (REDUCE ? 8 : 9);
+}
 
 template <int S, bool REDUCE>
-__global__ void __launch_bounds__(PUSH_BLOCK, S == POG_STORE_F64 ? 1 : 4) push_step_kernel(
+__global__ void __launch_bounds__(PUSH_BLOCK, (push_min_blocks<S, REDUCE>())) push_step_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ fin,
     typename Store<S>::E* __restrict__ fout, const uint32_t* __restrict__ flags,
     const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
@@ -86,6 +92,7 @@ extern "C" int pog_step_push(const pog_params* p, const void* f_in, void* f_out,
   if (rc) return rc;
   if (!f_in || !f_out || !flags) return set_error(POG_E_ARG, "f_in/f_out/flags is NULL");
   if (f_in == f_out) return set_error(POG_E_ARG, "push step needs distinct f_in and f_out");
+  if (p->density_ref) return set_error(POG_E_ARG, "the push step has no per-cell reference density form");
   if (p->les_mode == POG_LES_STENCIL && !u_prev)
     return set_error(POG_E_ARG, "LES stencil mode needs u_prev");
   KParams kp = make_kparams(p);

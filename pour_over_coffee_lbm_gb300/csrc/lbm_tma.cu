@@ -401,7 +401,7 @@ int launch_rows_step(const KParams& kp, int parity, bool reduce, void* f, const 
                      const int32_t* cells, int32_t ncells, const float* force, const float* pdrag, const float* eps,
                      const float* u_prev, float* u_next, float* rho_out, float* u_out, double* red,
                      cudaStream_t s) {
-  if (((uintptr_t)f & 15u) != 0u) return 1;
+  if (((uintptr_t)f & 15u) != 0u || kp.dref) return 1;
   switch (kp.storage) {
     case POG_STORE_F32:
       return rows_step_s<POG_STORE_F32>(kp, parity, reduce, f, flags, cells, ncells, force, pdrag, eps, u_prev, u_next, rho_out, u_out, red, s);

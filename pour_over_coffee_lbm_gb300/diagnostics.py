@@ -410,6 +410,8 @@ def save_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
          "deposit_mask": s._dmask.cpu().numpy()}
     if s._porosity is not None:
         d["porosity"] = s._porosity.cpu().numpy()
+    if s._dref is not None:
+        d["density_ref"] = s._dref.view(torch.int16).cpu().numpy()
     if s._ul is not None:
         d["u_les0"], d["u_les1"] = s._ul[0].cpu().numpy(), s._ul[1].cpu().numpy()
     if particles is not None:
@@ -441,7 +443,11 @@ def load_checkpoint(path: str, solver, particles=None, pour=None, filter_system=
     z = np.load(path)
     if tuple(z["shape"]) != (s.NX, s.NY, s.NZ) or int(z["storage"]) != s.cfg.storage:
         raise ValueError("checkpoint grid/storage does not match the solver")
+    if ("density_ref" in z) != (s._dref is not None):
+        raise ValueError("checkpoint and solver differ in the FP16S reference-density form")
     s._f.view(torch.uint8).copy_(torch.from_numpy(z["f"]))
+    if s._dref is not None:
+        s._dref.view(torch.int16).copy_(torch.from_numpy(z["density_ref"]))
     s._flags.copy_(torch.from_numpy(z["flags"]))
     s._force.copy_(torch.from_numpy(z["force"]))
     s._force_active = bool(z["force_active"])

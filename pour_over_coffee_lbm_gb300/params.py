@@ -49,6 +49,7 @@ class PogParams(ctypes.Structure):
         ("deposit_mask", ctypes.c_void_p),
         ("wall_cells", ctypes.c_void_p), ("n_wall_cells", ctypes.c_int32),
         ("step_kernel", ctypes.c_int32),
+        ("density_ref", ctypes.c_void_p),
     ]
 
 

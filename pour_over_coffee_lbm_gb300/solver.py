@@ -126,7 +126,7 @@ class GB300LBMSolver:
 
     def __init__(self, config: Optional[LatticeConfig] = None, device: str = "cuda",
                  porosity: Optional[np.ndarray] = None, preferred_backend: Optional[str] = None,
-                 step_kernel: str = "auto"):
+                 step_kernel: str = "auto", density_reference: bool = False):
         if not torch.cuda.is_available():
             raise RuntimeError("GB300LBMSolver needs a CUDA device (no CPU path exists)")
         self.lib = _lib.load()
@@ -151,6 +151,14 @@ class GB300LBMSolver:
             raise ValueError("step_kernel must be 'auto', 'rows' or 'registers'")
         self.step_kernel = step_kernel
         self._p.step_kernel = STEP_CELLS if step_kernel == "registers" else STEP_AUTO
+        # FP16S with a per-cell reference density (pog_params.density_ref): each slot is stored
+        # relative to its owner cell's density instead of rho0
+        self._dref = None
+        if density_reference:
+            if c.storage != STORE_F16S:
+                raise ValueError("density_reference needs FP16S storage")
+            self._dref = torch.zeros(self.n, dtype=torch.float16, device=self.device)
+            self._p.density_ref = self._dref.data_ptr()
         self._walls = None
         self._build_wall_list()
         self._f = torch.empty((19,) + shape, dtype=_STORAGE_DTYPE[c.storage], device=dev)
@@ -619,7 +627,7 @@ class GB300LBMSolver:
         self.cfg = self.cfg.replace(les_mode=mode, cs_smag=float(smagorinsky_constant))
         p = self.cfg.to_c()
         for name in ("inlet_control", "pour_control", "filter_blockage", "phase", "deposit_mask",
-                     "wall_cells", "n_wall_cells", "step_kernel", "tau_air"):
+                     "wall_cells", "n_wall_cells", "step_kernel", "density_ref", "tau_air"):
             setattr(p, name, getattr(self._p, name))
         self._p = p
         self.use_les = True

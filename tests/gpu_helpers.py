@@ -53,11 +53,16 @@ def wall_list(p, flags):
 class AARun:
     """AA-pattern state driven through pog_step."""
 
-    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None, rows=False, cells=False):
+    def __init__(self, cfg, flags=None, eps=None, force=None, pdrag=None, rows=False, cells=False,
+                 ref_density=False):
         self.cfg = cfg
         self.p = cfg.to_c()
         if cells:
             self.p.step_kernel = STEP_CELLS  # the per-cell kernel even where the two-cell one applies
+        self.dref = None
+        if ref_density:  # FP16S relative to per-cell reference densities (set by the init below)
+            self.dref = torch.zeros(cfg.ncell, dtype=torch.float16, device="cuda")
+            self.p.density_ref = self.dref.data_ptr()
         shape = (cfg.nz, cfg.ny, cfg.nx)
         self.flags = gpu_flags(cfg) if flags is None else torch.as_tensor(np.asarray(flags).astype(np.int32)).cuda()
         self.walls = None
