@@ -14,18 +14,22 @@ namespace pog {
 template <int S, int PARITY>
 __device__ __forceinline__ void aa_load(const KParams& kp, const typename Store<S>::E* __restrict__ f,
                                         uint32_t c, uint32_t fl, bool open, typename Store<S>::E raw[19]) {
+  // odd step: one 64-bit base per cell, each slot then one widening multiply-add of its 32-bit
+  // offset (measured 4 % faster on the 16-bit odd step; the even step keeps 32-bit element
+  // indices, which measured faster there)
+  const typename Store<S>::E* __restrict__ fc = f + c;
   if (PARITY == 0) {
 #pragma unroll
     for (int q = 0; q < 19; ++q) raw[q] = f[(uint32_t)q * kp.n + c];
   } else if (open) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) raw[q] = f[c + kp.rd[q]];
+    for (int q = 0; q < 19; ++q) raw[q] = fc[kp.rd[q]];
   } else {
     // source c - e_q is the neighbour in direction opp(q); a solid one bounces f_q back
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
       const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + opp(q))) & 1u);
-      raw[q] = f[c + (wall ? kp.pl[q] : kp.rd[q])];
+      raw[q] = fc[wall ? kp.pl[q] : kp.rd[q]];
     }
   }
 }
@@ -66,14 +70,15 @@ __device__ __forceinline__ void aa_update(const KParams& kp, typename Store<S>::
     for (int q = 0; q < 19; ++q) f[(uint32_t)opp(q) * n + c] = St::ench(fv[q]);
     return;
   }
+  typename St::E* __restrict__ fc = f + opaque(c);  // rebuilt, not held across the collision
   if (open) {
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[c + kp.wr[q]] = St::ench(fv[q]);
+    for (int q = 0; q < 19; ++q) fc[kp.wr[q]] = St::ench(fv[q]);
   } else {
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
       const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
-      f[c + (wall ? kp.pl[opp(q)] : kp.wr[q])] = St::ench(fv[q]);
+      fc[wall ? kp.pl[opp(q)] : kp.wr[q]] = St::ench(fv[q]);
     }
   }
 }
