@@ -87,4 +87,43 @@ __device__ __forceinline__ bool aa_live(const KParams& kp, uint32_t c, uint32_t 
   return !(fl & POG_CELL_SOLID) && c >= kp.guard_lo && c <= kp.guard_hi;
 }
 
+// The even AA step of one cell of FP16S stored relative to per-cell reference densities
+// (kp.dref): decode the cell's own slots with its reference, collide, set the reference to the new
+// density (FP16-rounded) and store the outputs relative to it.  Shared by the per-cell reference
+// kernel (lbm_ref.cu) and the two-cell even step (lbm_pair.cu) for the cells it does not pair.
+template <bool REDUCE>
+__device__ __forceinline__ void ref_even_cell(const KParams& kp, __half* __restrict__ f, uint32_t c, uint32_t fl,
+                                              const float* __restrict__ force, const float* __restrict__ pdrag,
+                                              const float* __restrict__ eps, const float* __restrict__ u_prev,
+                                              float* __restrict__ u_next, float* __restrict__ rho_out,
+                                              float* __restrict__ u_out, RedAcc<float>& acc) {
+  using St = Store<POG_STORE_F16S>;
+  const uint32_t n = kp.n;
+  const float dc = __half2float(kp.dref[c]);
+  float fv[19];
+#pragma unroll
+  for (int q = 0; q < 19; ++q) fv[q] = St::dech(f[(uint32_t)q * n + c]);
+  float nu_st = 0.0f;
+  if (kp.les_mode == POG_LES_STENCIL && !(fl & POG_CELL_POROUS)) nu_st = les_nu_stencil<float>(kp, c, u_prev);
+  const CellResult<float> r =
+      collide_cell<float, true>(kp, fl, c, fv, force, pdrag, eps, nu_st, St::SCALE, kp.rho0 + dc);
+  if (rho_out) rho_out[c] = r.rho;
+  if (u_out) {
+    u_out[c] = r.ux;
+    u_out[n + c] = r.uy;
+    u_out[2u * n + c] = r.uz;
+  }
+  if (u_next) {
+    u_next[c] = r.ux;
+    u_next[n + c] = r.uy;
+    u_next[2u * n + c] = r.uz;
+  }
+  if (REDUCE) acc.add(r);
+  const __half dnew = __float2half_rn(r.rho - kp.rho0);
+  const float shift = (__half2float(dnew) - dc) * F16_SCALE;
+#pragma unroll
+  for (int q = 0; q < 19; ++q) f[(uint32_t)opp(q) * n + c] = St::ench(__fmaf_rn(-(float)wd(q), shift, fv[q]));
+  kp.dref[c] = dnew;
+}
+
 }  // namespace pog

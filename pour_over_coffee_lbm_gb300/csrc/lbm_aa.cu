@@ -263,11 +263,15 @@ int pog_step(const pog_params* p, void* f, const uint32_t* flags, long long t, i
     const int parity = (int)((t + i) & 1);
     // the row-tiled kernel when the caller supplied the bounce-back cell list (and it applies)
     rc = 1;
-    if (kp.dref)
-      rc = launch_ref_step(kp, parity, reductions != nullptr, false, f, flags, force, pdrag, porosity,
-                           stencil ? up : nullptr, stencil ? un : nullptr, last ? rho_out : nullptr,
-                           last ? u_out : nullptr, reductions, s);
-    else if (p->wall_cells)
+    if (kp.dref) {
+      if (p->step_kernel == POG_STEP_AUTO && !stencil)
+        rc = launch_pair_step(kp, parity, reductions != nullptr, f, flags, force, pdrag, porosity,
+                              last ? rho_out : nullptr, last ? u_out : nullptr, reductions, s);
+      if (rc == 1)
+        rc = launch_ref_step(kp, parity, reductions != nullptr, false, f, flags, force, pdrag, porosity,
+                             stencil ? up : nullptr, stencil ? un : nullptr, last ? rho_out : nullptr,
+                             last ? u_out : nullptr, reductions, s);
+    } else if (p->wall_cells)
       rc = launch_rows_step(kp, parity, reductions != nullptr, f, flags, p->wall_cells, p->n_wall_cells, force,
                             pdrag, porosity, stencil ? up : nullptr, stencil ? un : nullptr,
                             last ? rho_out : nullptr, last ? u_out : nullptr, reductions, s);

@@ -116,7 +116,10 @@ __device__ __forceinline__ void collide_dir2(uint32_t w[19], F2 ux, F2 uy, F2 uz
   w[P] = Pair16<S>::pack(fma2(keep, hp, sub2(sym, asym)));
 }
 
-template <int S, bool REDUCE>
+// REF: FP16S stored relative to per-cell reference densities (kp.dref, see lbm_ref.cu): each
+// lane decodes with its cell's reference, sets it to the new density and shifts its outputs to it
+// (folded into the collision's per-class constant terms).
+template <int S, bool REDUCE, bool REF>
 __global__ void __launch_bounds__(PAIR_BLOCK, (pair_min_blocks<REDUCE>())) aa_pair_even_kernel(
     const KParams kp, typename Store<S>::E* __restrict__ f, const uint32_t* __restrict__ flags,
     const float* __restrict__ force, const float* __restrict__ pdrag, const float* __restrict__ eps,
@@ -141,13 +144,17 @@ __global__ void __launch_bounds__(PAIR_BLOCK, (pair_min_blocks<REDUCE>())) aa_pa
       for (int lane = 0; lane < 2; ++lane) {
         const uint32_t c = c0 + (uint32_t)lane, flc = lane ? fl.y : fl.x;
         if (!(lane ? l1 : l0)) continue;
-        typename St::E raw[19];
-        aa_load<S, 0>(kp, f, c, flc, false, raw);
-        float fv[19];
+        if constexpr (REF) {
+          ref_even_cell<REDUCE>(kp, f, c, flc, force, pdrag, eps, nullptr, nullptr, rho_out, u_out, acc);
+        } else {
+          typename St::E raw[19];
+          aa_load<S, 0>(kp, f, c, flc, false, raw);
+          float fv[19];
 #pragma unroll
-        for (int q = 0; q < 19; ++q) fv[q] = St::dech(raw[q]);
-        aa_update<S, 0, REDUCE, false>(kp, f, c, flc, false, fv, force, pdrag, eps, nullptr, nullptr, rho_out,
-                                            u_out, acc);
+          for (int q = 0; q < 19; ++q) fv[q] = St::dech(raw[q]);
+          aa_update<S, 0, REDUCE, false>(kp, f, c, flc, false, fv, force, pdrag, eps, nullptr, nullptr, rho_out,
+                                         u_out, acc);
+        }
       }
       continue;
     }
@@ -189,7 +196,24 @@ __global__ void __launch_bounds__(PAIR_BLOCK, (pair_min_blocks<REDUCE>())) aa_pa
     const float sc = St::SCALE, inv_sc = 1.0f / St::SCALE;  // powers of two: exact
     const F2 SC = sp2(sc);
     const F2 drho = mul2(SC, rsum);
-    const F2 rho = add2(sp2(kp.rho0), drho);
+    // the cells' shift densities: rho0, or their references rho0 + d_c
+    F2 dd = sp2(0.0f);
+    if constexpr (REF) {
+      __half2 h;
+      const uint32_t dw = reinterpret_cast<const uint32_t*>(kp.dref)[c0 >> 1];
+      memcpy(&h, &dw, 4);
+      dd = __half22float2(h);
+    }
+    const F2 rho = add2(add2(sp2(kp.rho0), dd), drho);
+    // REF: the new references (this step's densities, FP16-rounded) and the shift of the outputs
+    // to them, in stored units
+    uint32_t dnew_w = 0u;
+    F2 dshift = sp2(0.0f);
+    if constexpr (REF) {
+      const __half2 dn = __float22half2_rn(sub2(rho, sp2(kp.rho0)));
+      memcpy(&dnew_w, &dn, 4);
+      dshift = mul2(sub2(__half22float2(dn), dd), sp2(F16_SCALE));
+    }
     const F2 mx = mul2(SC, mxs), my = mul2(SC, mys), mz = mul2(SC, mzs);
     F2 Gx = mul2(rho, sp2(kp.gx)), Gy = mul2(rho, sp2(kp.gy)), Gz = mul2(rho, sp2(kp.gz));
     if (force) {
@@ -260,14 +284,14 @@ __global__ void __launch_bounds__(PAIR_BLOCK, (pair_min_blocks<REDUCE>())) aa_pa
       const F2 b3_1 = mul2(As, sp2((float)(3.0 / 18.0))), b3_2 = mul2(As, sp2((float)(3.0 / 36.0)));
       const F2 nuF = mul2(sp2(-1.0f), uF);
       const F2 h0 = Pk::unpack(opaque(w[0]));
-      w[0] = Pk::pack(fma2(keep, h0, fma2(As, nuF, mul2(a1_0, base))));
+      w[0] = Pk::pack(fma2(keep, h0, fma2(sp2(-(float)(1.0 / 3.0)), dshift, fma2(As, nuF, mul2(a1_0, base)))));
       PairCoef2 k1, k2;
-      k1.A = fma2(b3_1, nuF, mul2(a1_1, base));
+      k1.A = fma2(sp2(-(float)(1.0 / 18.0)), dshift, fma2(b3_1, nuF, mul2(a1_1, base)));
       k1.B = mul2(sp2(4.5f), a1_1);
       k1.Cc = mul2(sp2(3.0f), b3_1);
       k1.D = mul2(sp2(3.0f), a1_1);
       k1.b3 = b3_1;
-      k2.A = fma2(b3_2, nuF, mul2(a1_2, base));
+      k2.A = fma2(sp2(-(float)(1.0 / 36.0)), dshift, fma2(b3_2, nuF, mul2(a1_2, base)));
       k2.B = mul2(sp2(4.5f), a1_2);
       k2.Cc = mul2(sp2(3.0f), b3_2);
       k2.D = mul2(sp2(3.0f), a1_2);
@@ -321,21 +345,27 @@ __global__ void __launch_bounds__(PAIR_BLOCK, (pair_min_blocks<REDUCE>())) aa_pa
     if (paired) {
 #pragma unroll
       for (int q = 0; q < 19; ++q) fw[(kp.pl[opp(q)] + cs) >> 1] = w[q];
+      if constexpr (REF) reinterpret_cast<uint32_t*>(kp.dref)[cs >> 1] = dnew_w;
     } else {
 #pragma unroll
       for (int q = 0; q < 19; ++q) {
         if (l0) fh[kp.pl[opp(q)] + cs] = (uint16_t)w[q];
         if (l1) fh[kp.pl[opp(q)] + cs + 1u] = (uint16_t)(w[q] >> 16);
       }
+      if constexpr (REF) {
+        uint16_t* dh = reinterpret_cast<uint16_t*>(kp.dref);
+        if (l0) dh[cs] = (uint16_t)dnew_w;
+        if (l1) dh[cs + 1u] = (uint16_t)(dnew_w >> 16);
+      }
     }
   }
   if (REDUCE) reduce_add<float>(acc, red);
 }
 
-template <int S, bool REDUCE>
+template <int S, bool REDUCE, bool REF = false>
 static int launch_pair(const KParams& kp, void* f, const uint32_t* flags, const float* force, const float* pdrag,
                        const float* eps, float* rho_out, float* u_out, double* red, cudaStream_t s) {
-  auto kern = aa_pair_even_kernel<S, REDUCE>;
+  auto kern = aa_pair_even_kernel<S, REDUCE, REF>;
   static thread_local int grid = 0;
   if (grid == 0) grid = persistent_blocks((const void*)kern, PAIR_BLOCK);
   if (grid <= 0) return set_error(POG_E_CUDA, "occupancy query failed");
@@ -358,10 +388,14 @@ int launch_pair_step(const KParams& kp, int parity, bool reduce, void* f, const 
                      double* red, cudaStream_t s) {
   if (parity != 0) return 1;
   if (kp.storage != POG_STORE_F16S && kp.storage != POG_STORE_BF16S) return 1;
-  if (kp.dref) return 1;  // the per-cell reference form runs in lbm_ref.cu
   if ((kp.nx & 1u) || kp.les_mode == POG_LES_STENCIL || kp.forcing_mode != POG_FORCING_GUO || kp.phase) return 1;
   if (!aligned(f, 4) || !aligned(flags, 8) || !aligned(force, 8) || !aligned(rho_out, 8) || !aligned(u_out, 8))
     return 1;
+  if (kp.dref) {  // FP16S relative to per-cell reference densities
+    if (kp.storage != POG_STORE_F16S || !aligned(kp.dref, 4)) return 1;
+    return reduce ? launch_pair<POG_STORE_F16S, true, true>(kp, f, flags, force, pdrag, eps, rho_out, u_out, red, s)
+                  : launch_pair<POG_STORE_F16S, false, true>(kp, f, flags, force, pdrag, eps, rho_out, u_out, red, s);
+  }
   if (kp.storage == POG_STORE_F16S)
     return reduce ? launch_pair<POG_STORE_F16S, true>(kp, f, flags, force, pdrag, eps, rho_out, u_out, red, s)
                   : launch_pair<POG_STORE_F16S, false>(kp, f, flags, force, pdrag, eps, rho_out, u_out, red, s);

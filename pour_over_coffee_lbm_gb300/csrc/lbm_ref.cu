@@ -52,6 +52,10 @@ __global__ void __launch_bounds__(REF_BLOCK, (ref_min_blocks<PARITY, REDUCE>()))
   for (uint32_t c = blockIdx.x * REF_BLOCK + threadIdx.x; c < n; c += gridDim.x * REF_BLOCK) {
     const uint32_t fl = flags[c];
     if (!aa_live(kp, c, fl)) continue;
+    if (PARITY == 0 && !MACRO_ONLY) {
+      ref_even_cell<REDUCE>(kp, f, c, fl, force, pdrag, eps, u_prev, u_next, rho_out, u_out, acc);
+      continue;
+    }
     const bool open = PARITY == 1 && __all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u);
     __half raw[19];
     aa_load<POG_STORE_F16S, PARITY>(kp, f, c, fl, open, raw);
@@ -98,17 +102,7 @@ __global__ void __launch_bounds__(REF_BLOCK, (ref_min_blocks<PARITY, REDUCE>()))
       u_next[2u * n + c] = r.uz;
     }
     if (REDUCE) acc.add(r);
-    if (MACRO_ONLY) continue;
-    if (PARITY == 0) {
-      // the new reference: this step's density, rounded to FP16; outputs moved to it
-      const __half dnew = __float2half_rn(r.rho - kp.rho0);
-      const float shift = (__half2float(dnew) - dc) * F16_SCALE;
-#pragma unroll
-      for (int q = 0; q < 19; ++q)
-        f[(uint32_t)opp(q) * n + c] = St::ench(__fmaf_rn(-(float)wd(q), shift, fv[q]));
-      dref[c] = dnew;
-      continue;
-    }
+    if (MACRO_ONLY || PARITY == 0) continue;  // (the even step's update is ref_even_cell)
     // outgoing: slot q goes to c + e_q (shift of neighbour c + e_q), slot opp Q to c - e_Q; a
     // bounced slot is c's own (its shift is zero)
     const uint32_t c2 = opaque(c);
