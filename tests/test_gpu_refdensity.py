@@ -140,3 +140,38 @@ def test_rejected_uses(cuda):
     with pytest.raises(ValueError):
         from pour_over_coffee_lbm_gb300 import GB300LBMSolver
         GB300LBMSolver(_cfg(storage=STORE_F32), density_reference=True)
+
+
+def test_stencil_les_and_particles(cuda):
+    """The per-cell reference form with the LES stencil mode (per-cell kernel on both steps) and
+    with two-way coupled particles (their deposit cells take the per-cell path of the two-cell
+    even step): both stay with plain FP16S to FP16 rounding."""
+    from pour_over_coffee_lbm_gb300 import CoffeeParticleSystem, GB300LBMSolver, ParticleConfig
+    from pour_over_coffee_lbm_gb300.params import LES_STENCIL
+    cfg = _cfg(nx=40, ny=40, nz=40, les_mode=LES_STENCIL)
+    out = []
+    for ref in (False, True):
+        s = GB300LBMSolver(cfg, density_reference=ref)
+        s.run(59)
+        s.run(1, want_macro=True)
+        out.append(s)
+    fluid = ((out[0].flags & CELL_SOLID) == 0)
+    e = rel_l2(out[1]._u[:, fluid].cpu().numpy(), out[0]._u[:, fluid].cpu().numpy())
+    print("LES stencil, reference vs plain FP16S after 60 steps: u rel L2 %.2e" % e)
+    assert out[1].check_stability() and e < 5e-3
+    cfg = _cfg(nx=48, ny=48, nz=48)
+    pc = ParticleConfig(count=3000, deterministic=True)
+    runs = []
+    for ref in (False, True):
+        s = GB300LBMSolver(cfg, density_reference=ref)
+        ps = CoffeeParticleSystem(max_particles=pc.count, lattice=cfg, config=pc)
+        ps.seed()
+        for _ in range(40):
+            s.step_with_two_way_coupling(ps)
+        s.run(1, want_macro=True)
+        runs.append((s, ps))
+    fluid = ((runs[0][0].flags & CELL_SOLID) == 0)
+    e = rel_l2(runs[1][0]._u[:, fluid].cpu().numpy(), runs[0][0]._u[:, fluid].cpu().numpy())
+    dp = (runs[1][1]._pos[:, :pc.count] - runs[0][1]._pos[:, :pc.count]).abs().max().item()
+    print("coupled, reference vs plain FP16S after 40 steps: u rel L2 %.2e, particle max |dx| %.1e" % (e, dp))
+    assert runs[1][0].check_stability() and e < 5e-3 and dp < 1e-2
