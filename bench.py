@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--precision-only", choices=["fp32", "fp16s", "bf16s"], default=None,
                     help="time only the 256^3 precision case in this storage for --steps steps (profiling)")
     ap.add_argument("--precision-case", choices=["les_band", "plain"], default="les_band")
+    ap.add_argument("--coupled-only", action="store_true",
+                    help="print only the coupled 128^3 / 20,000-particle line (profiling)")
     ap.add_argument("--scale-only", action="store_true",
                     help="run --steps coupled steps of the 320x320x384 / 1M-particle case (profiling)")
     ap.add_argument("--step-kernel", choices=["auto", "rows", "registers"], default="auto",
@@ -993,10 +995,19 @@ def run_precision_only(args):
     print(json.dumps({"precision_only": args.precision_only, "step_kernel": args.step_kernel, **out}), flush=True)
 
 
+def run_coupled_only(args):
+    import torch
+    torch.cuda.set_device(0)
+    args.no_cpu = True
+    print(json.dumps({"coupled_only": coupled_line(args, peaks())}), flush=True)
+
+
 def main():
     args = parse()
     if args.precision_only:
         run_precision_only(args)
+    elif args.coupled_only:
+        run_coupled_only(args)
     elif args.scale_only:
         run_scale_only(args)
     elif args.impl == "reference":
