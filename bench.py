@@ -436,7 +436,8 @@ def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="auto"):
     """320x320x384 FP16S + LES + band + 1,000,000 particles: exactly `steps` two-way coupled steps
     (4 eager, the rest graph-replayed), then the outflow adjoint over the last adj_steps of them
     (recomputed in FP32 from the FP16S state exported at step steps - adj_steps, checkpoints every
-    ckpt).  Roofline fractions: the coupled step at 77 B per cell update (FP16S lattice) plus 268 B
+    ckpt).  Roofline fractions: the coupled step at 93 B per cell update (FP16S lattice 77 B, and the
+    rho/u the coupling pass gathers from, 16 B, written by the step) plus 268 B
     per particle (gather, drag, integration, deposit), the adjoint at 458 B per cell update (one
     forward recomputation, the state and the adjoint state read and written)."""
     import torch
@@ -483,7 +484,7 @@ def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="auto"):
     stable = bool(s.check_stability())
     done = s.t
     per_step = el / timed
-    fwd_bytes = 77 * cfg.ncell + 268 * pc.count
+    fwd_bytes = (77 + 16) * cfg.ncell + 268 * pc.count
     fwd_gbs = fwd_bytes / per_step / 1e9
     del g, s, ps
     torch.cuda.empty_cache()
@@ -507,7 +508,7 @@ def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="auto"):
            "coupled_ms_per_step": round(per_step * 1e3, 4), "stable": stable,
            "coupled_roofline": {"algorithmic_bytes_per_step": fwd_bytes, "achieved_gbs": round(fwd_gbs, 1),
                                 "frac": round(fwd_gbs / peak[0], 4), "peak": peak[0], "peak_source": peak[1],
-                                "bytes": "77 B per cell update + 268 B per particle"},
+                                "bytes": "77 B per cell update (FP16S) + 16 B rho/u write + 268 B per particle"},
            "adjoint": {"steps": adj_steps, "forward_ms": round(fwd * 1e3, 1), "backward_ms": round(bwd * 1e3, 1),
                        "adjoint_mlups": round(cfg.ncell * adj_steps / bwd / 1e6, 1), "loss": J,
                        "roofline": {"achieved_gbs": round(adj_gbs, 1), "frac": round(adj_gbs / peak[0], 4),
