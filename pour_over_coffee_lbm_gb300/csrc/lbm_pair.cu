@@ -31,11 +31,12 @@
 namespace pog {
 
 constexpr int PAIR_BLOCK = 128;
-// Resident 128-thread blocks per SM: 7 (72 registers, a few spilled bytes; 54.1 GLUPS FP16S at
-// 256^3 against 53.0 at 80 registers) for the plain step, 6 (80) with the FP64 sums.
+// Resident 128-thread blocks per SM: 8 (64 registers, 56 spilled bytes: 274 us per 256^3 even
+// step against 276 at 72 registers and 282 at 80, which spills nothing) for the plain step, 6 (80)
+// with the FP64 sums.
 template <bool REDUCE>
 constexpr int pair_min_blocks() {
-  return REDUCE ? 6 : 7;
+  return REDUCE ? 6 : 8;
 }
 
 using F2 = float2;  // .x = cell c0, .y = cell c0 + 1

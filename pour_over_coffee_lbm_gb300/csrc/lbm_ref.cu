@@ -27,12 +27,12 @@ namespace pog {
 
 constexpr int REF_BLOCK = 128;
 
-// resident 128-thread blocks per SM: 9 (56 registers) for the even step, 7 (72, the fewest that
-// compile without spilling) for the odd step with its neighbour shifts, 8 (64) for the variants
-// with the FP64 sums
+// resident 128-thread blocks per SM: 9 (56 registers) for the even step, 8 (64, a few spilled
+// bytes; 451 us per 256^3 odd step against 461 at 72 registers, which spills nothing) for the odd
+// step with its neighbour shifts and for the variants with the FP64 sums
 template <int PARITY, bool REDUCE>
 constexpr int ref_min_blocks() {
-  return REDUCE ? 8 : (PARITY == 1 ? 7 : 9);
+  return REDUCE ? 8 : (PARITY == 1 ? 8 : 9);
 }
 
 // the representative Q of the k-th direction pair (Q, opp Q)
