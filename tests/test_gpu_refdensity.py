@@ -74,6 +74,15 @@ def test_export_import_round_trip(cuda, steps):
     _advance(r, steps)
     nat = r.natural(np.float64)
     assert np.isfinite(nat).all()
+    # the export's decoding (each slot with its owner's reference) against the macroscopic pass's
+    # (its own code path, which moves every streamed slot to the reading cell's reference)
+    rho = torch.empty_like(r.rho)
+    _lib.check(lib().pog_macroscopic(ctypes.byref(r.p), P(r.f), P(r.flags), r.t, None, None, P(rho), None, S()))
+    torch.cuda.synchronize()
+    fluid = ((r.flags & CELL_SOLID) == 0).cpu().numpy()
+    inlet_outlet = ((r.flags & 0x06) != 0).cpu().numpy()  # their rho is imposed, not summed
+    keep = fluid & ~inlet_outlet
+    assert np.abs(nat.sum(0)[keep] - rho.cpu().numpy()[keep]).max() < 1e-6
     if steps % 2:
         return  # import writes an even-parity state
     f2 = torch.empty_like(r.f)
@@ -175,3 +184,16 @@ def test_stencil_les_and_particles(cuda):
     dp = (runs[1][1]._pos[:, :pc.count] - runs[0][1]._pos[:, :pc.count]).abs().max().item()
     print("coupled, reference vs plain FP16S after 40 steps: u rel L2 %.2e, particle max |dx| %.1e" % (e, dp))
     assert runs[1][0].check_stability() and e < 5e-3 and dp < 1e-2
+
+
+def test_odd_nx_per_cell_even_step(cuda):
+    """An odd nx keeps the even step per cell (ref_even_cell) in the reference form too."""
+    cfg = LatticeConfig(nx=37, ny=29, nz=41, band_thickness=2.5, cone_apex_z=5.5, center_x=17.25, center_y=13.0,
+                        cone_half_angle_deg=35.0, inlet_radius=7.5, hole_radius=1.5, les_mode=LES_LOCAL,
+                        storage=STORE_F16S)
+    ref = _ref_run(cfg)
+    _advance(ref, 40)
+    plain = AARun(cfg)
+    _advance(plain, 40)
+    fluid = ((ref.flags & CELL_SOLID) == 0).cpu().numpy()
+    assert rel_l2(ref.u.cpu().numpy()[:, fluid], plain.u.cpu().numpy()[:, fluid]) < 5e-3
