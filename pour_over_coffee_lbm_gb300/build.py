@@ -27,7 +27,7 @@ SOURCES = {
     "lbm_push.cu": [],
     "particles.cu": ["-fmad=false"],
     "particles_noalloc.cu": [],
-    "adjoint.cu": [],
+    "adjoint.cu": FAST_F32,
     "pour.cu": [],
     "diag.cu": [],
     "filter.cu": ["-fmad=false"],

@@ -25,49 +25,61 @@
 namespace pog {
 
 constexpr int ADJ_BLOCK = 256;
-
-// d(sum_q lam_q feq_q)/d(rho, u) for feq at (rho, u): returns bar_rho, bar_u.
-template <typename C>
-__device__ __forceinline__ void eq_vjp(const C lam[19], C rho, C ux, C uy, C uz, C& brho, C& bux,
-                                       C& buy, C& buz) {
-  C br = 0, bx = 0, by = 0, bz = 0;
-  const C usq = ux * ux + uy * uy + uz * uz;
-#pragma unroll
-  for (int q = 0; q < 19; ++q) {
-    const C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
-    const C wl = (C)wd(q) * lam[q];
-    br += wl * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - (C)1.5 * usq);
-    const C g = wl * rho * ((C)3 + (C)9 * eu);
-    bx += g * (C)cx(q) - wl * rho * (C)3 * ux;
-    by += g * (C)cy(q) - wl * rho * (C)3 * uy;
-    bz += g * (C)cz(q) - wl * rho * (C)3 * uz;
-  }
-  brho = br;
-  bux = bx;
-  buy = by;
-  buz = bz;
+// The adjoint step kernel: 128-thread blocks, 5 resident per SM for FP32 (96 registers, no spill:
+// 20 warps per SM against 16 at 256 x 2 and 128 registers), FP64 at its register need (221).
+constexpr int ADJ_STEP_BLOCK = 128;
+template <int S>
+constexpr int adj_min_blocks() {
+  return S == POG_STORE_F64 ? 1 : 5;
 }
 
-// eq_vjp for lam_q = a_q - b_q (not stored)
+// Weighted lattice moments of a direction vector a_q: m0 = sum w_q a_q, m1_a = sum w_q a_q e_qa,
+// m2_ab = sum w_q a_q e_qa e_qb.  Every sum over q in the reverse step below is a polynomial of
+// degree <= 2 in e_q times w_q a_q, so it is a contraction of these ten numbers (formed once per
+// cell from the opposite-pair sums and differences) instead of a 19-term loop of its own.
 template <typename C>
-__device__ __forceinline__ void eq_vjp_diff(const C a[19], const C b[19], C rho, C ux, C uy, C uz, C& brho,
-                                            C& bux, C& buy, C& buz) {
-  C br = 0, bx = 0, by = 0, bz = 0;
-  const C usq = ux * ux + uy * uy + uz * uz;
+struct WMom {
+  C m0, x, y, z, xx, yy, zz, xy, xz, yz;
+};
+
+template <typename C>
+__device__ __forceinline__ WMom<C> wmoments(const C a[19]) {
+  WMom<C> M;
+  M.m0 = (C)wd(0) * a[0];
+  M.x = M.y = M.z = M.xx = M.yy = M.zz = M.xy = M.xz = M.yz = (C)0;
 #pragma unroll
-  for (int q = 0; q < 19; ++q) {
-    const C eu = (C)cx(q) * ux + (C)cy(q) * uy + (C)cz(q) * uz;
-    const C wl = (C)wd(q) * (a[q] - b[q]);
-    br += wl * ((C)1 + (C)3 * eu + (C)4.5 * eu * eu - (C)1.5 * usq);
-    const C g = wl * rho * ((C)3 + (C)9 * eu);
-    bx += g * (C)cx(q) - wl * rho * (C)3 * ux;
-    by += g * (C)cy(q) - wl * rho * (C)3 * uy;
-    bz += g * (C)cz(q) - wl * rho * (C)3 * uz;
+  for (int q = 1; q < 19; ++q) {
+    if (q > opp(q)) continue;  // each opposite pair once: e_opp = -e_q
+    const C w = (C)wd(q);
+    const C sp = a[q] + a[opp(q)], dm = a[q] - a[opp(q)];
+    M.m0 += w * sp;
+    if (cx(q)) M.x += (C)cx(q) * w * dm;
+    if (cy(q)) M.y += (C)cy(q) * w * dm;
+    if (cz(q)) M.z += (C)cz(q) * w * dm;
+    if (cx(q)) M.xx += w * sp;
+    if (cy(q)) M.yy += w * sp;
+    if (cz(q)) M.zz += w * sp;
+    if (cx(q) && cy(q)) M.xy += (C)(cx(q) * cy(q)) * w * sp;
+    if (cx(q) && cz(q)) M.xz += (C)(cx(q) * cz(q)) * w * sp;
+    if (cy(q) && cz(q)) M.yz += (C)(cy(q) * cz(q)) * w * sp;
   }
-  brho = br;
-  bux = bx;
-  buy = by;
-  buz = bz;
+  return M;
+}
+
+// d(sum_q lam_q feq_q)/d(rho, u) for feq at (rho, u), from the weighted moments M of lam:
+// sum_q w lam (1 + 3 e.u + 4.5 (e.u)^2 - 1.5 u.u) and rho sum_q w lam ((3 + 9 e.u) e - 3 u).
+template <typename C>
+__device__ __forceinline__ void eq_vjp(const WMom<C>& M, C rho, C ux, C uy, C uz, C& brho, C& bux, C& buy,
+                                       C& buz) {
+  const C usq = ux * ux + uy * uy + uz * uz;
+  const C Mux = M.xx * ux + M.xy * uy + M.xz * uz;
+  const C Muy = M.xy * ux + M.yy * uy + M.yz * uz;
+  const C Muz = M.xz * ux + M.yz * uy + M.zz * uz;
+  brho = M.m0 * ((C)1 - (C)1.5 * usq) + (C)3 * (ux * M.x + uy * M.y + uz * M.z) +
+         (C)4.5 * (ux * Mux + uy * Muy + uz * Muz);
+  bux = rho * ((C)3 * M.x + (C)9 * Mux - (C)3 * ux * M.m0);
+  buy = rho * ((C)3 * M.y + (C)9 * Muy - (C)3 * uy * M.m0);
+  buz = rho * ((C)3 * M.z + (C)9 * Muz - (C)3 * uz * M.m0);
 }
 
 // Inlet cell c (f* = feq(rho, (0, 0, u_z(a)))): bar f (all directions equal) from the pulled
@@ -76,7 +88,7 @@ template <typename C>
 __device__ __forceinline__ C adj_inlet_cell(const KParams& kp, uint32_t c, const C ls[19], C rho, C mu_z, double g[16]) {
   const C uz = inlet_uz<C>(kp, c);
   C brho, bux, buy, buz;
-  eq_vjp<C>(ls, rho, (C)0, (C)0, uz, brho, bux, buy, buz);
+  eq_vjp<C>(wmoments<C>(ls), rho, (C)0, (C)0, uz, brho, bux, buy, buz);
   buz += mu_z;  // the cell's output velocity (0, 0, u_z) read by the next step's LES stencil
   // uz = u_inlet (1 + sum a_k T_k(s)), s = 2 r / R - 1
   const uint32_t i = c % kp.nx, j = (c / kp.nx) % kp.ny;
@@ -158,7 +170,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
 }
 
 template <int S>
-__global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint_kernel(
+__global__ void __launch_bounds__(ADJ_STEP_BLOCK, (adj_min_blocks<S>())) adjoint_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
     const uint32_t* __restrict__ flags, const float* __restrict__ eps, const float* __restrict__ pdrag,
@@ -173,7 +185,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
   __shared__ double ginl[POG_INLET_NCOEF];
   if (threadIdx.x < POG_INLET_NCOEF) ginl[threadIdx.x] = 0.0;
   __syncthreads();
-  for (uint32_t c = blockIdx.x * ADJ_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_BLOCK) {
+  for (uint32_t c = blockIdx.x * ADJ_STEP_BLOCK + threadIdx.x; c < n; c += gridDim.x * ADJ_STEP_BLOCK) {
     const uint32_t fl = flags[c];
     if (bar_nu) bar_nu[c] = (C)0;  // dJ/dnu of the cells whose stencil nu is live, below
     if ((fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) {
@@ -215,7 +227,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
     } else if (fl & POG_CELL_OUTLET) {
       const C ux = mx / rho, uy = my / rho, uz = mz / rho;
       C br_out, bux, buy, buz;
-      eq_vjp<C>(ls, (C)kp.rho_out, ux, uy, uz, br_out, bux, buy, buz);
+      eq_vjp<C>(wmoments<C>(ls), (C)kp.rho_out, ux, uy, uz, br_out, bux, buy, buz);
       (void)br_out;
       bux += mux;
       buy += muy;
@@ -328,29 +340,25 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       const C A = (C)1 - (C)0.5 * omega;
       const C uF = ux * Fx + uy * Fy + uz * Fz;
       // ---- reverse ----
-      // bar f_eq = lam* - bar neq is formed where it is used (eq_vjp_diff)
-      C* const bneq = bf;
-      C bomega = 0, bA = 0;
-      C bux = 0, buy = 0, buz = 0, bFx = 0, bFy = 0, bFz = 0;
+      // f* = f_eq + (1 - omega) neq + A w_q B_q, neq = f - f_eq.  Every sum over q below is a
+      // contraction of the weighted moments L of lam* (the sums of w lam* times 1, e_a, e_a e_b).
+      C bomega = 0;
 #pragma unroll
-      for (int q = 0; q < 19; ++q) {
-        const C lq = ls[q];
-        bneq[q] = ((C)1 - omega) * lq;
-        bomega -= lq * neq[q];
-        const C ex = (C)cx(q), ey = (C)cy(q), ez = (C)cz(q);
-        const C eu = ex * ux + ey * uy + ez * uz;
-        const C eF = ex * Fx + ey * Fy + ez * Fz;
-        const C Bq = (C)3 * (eF - uF) + (C)9 * eu * eF;
-        const C w = (C)wd(q);
-        bA += lq * w * Bq;
-        const C bB = lq * A * w;
-        bFx += bB * ((C)3 * (ex - ux) + (C)9 * eu * ex);
-        bFy += bB * ((C)3 * (ey - uy) + (C)9 * eu * ey);
-        bFz += bB * ((C)3 * (ez - uz) + (C)9 * eu * ez);
-        bux += bB * ((C)-3 * Fx + (C)9 * eF * ex);
-        buy += bB * ((C)-3 * Fy + (C)9 * eF * ey);
-        buz += bB * ((C)-3 * Fz + (C)9 * eF * ez);
-      }
+      for (int q = 0; q < 19; ++q) bomega -= ls[q] * neq[q];
+      const WMom<C> L = wmoments<C>(ls);
+      // the forcing term S_q = A w_q B_q, B_q = 3 (e.F - u.F) + 9 (e.u)(e.F)
+      const C L2ux = L.xx * ux + L.xy * uy + L.xz * uz, L2uy = L.xy * ux + L.yy * uy + L.yz * uz,
+              L2uz = L.xz * ux + L.yz * uy + L.zz * uz;
+      const C L2Fx = L.xx * Fx + L.xy * Fy + L.xz * Fz, L2Fy = L.xy * Fx + L.yy * Fy + L.yz * Fz,
+              L2Fz = L.xz * Fx + L.yz * Fy + L.zz * Fz;
+      const C bA = (C)3 * (Fx * L.x + Fy * L.y + Fz * L.z - uF * L.m0) +
+                   (C)9 * (ux * L2Fx + uy * L2Fy + uz * L2Fz);
+      const C bFx = A * ((C)3 * (L.x - ux * L.m0) + (C)9 * L2ux);
+      const C bFy = A * ((C)3 * (L.y - uy * L.m0) + (C)9 * L2uy);
+      const C bFz = A * ((C)3 * (L.z - uz * L.m0) + (C)9 * L2uz);
+      C bux = A * ((C)-3 * Fx * L.m0 + (C)9 * L2Fx);
+      C buy = A * ((C)-3 * Fy * L.m0 + (C)9 * L2Fy);
+      C buz = A * ((C)-3 * Fz * L.m0 + (C)9 * L2Fz);
       bomega += (C)-0.5 * bA;
       const C btau = -bomega / (tau * tau);
       if (st_live && bar_nu) bar_nu[c] = (C)3 * btau;
@@ -358,6 +366,8 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       bux += mux;
       buy += muy;
       buz += muz;
+      // bar neq_q = (1 - omega) lam*_q + e_q^T bP e_q (LES local: tau through Pi_neq)
+      C bPxx = 0, bPyy = 0, bPzz = 0, bPxy = 0, bPxz = 0, bPyz = 0;
       if (les_live) {
         const C bnu = (C)3 * btau;
         const C btl = bnu / (C)3;
@@ -366,17 +376,30 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
         const C bQ = bR * (C)9 * cs2 / (rho * Rr);
         brho += bR * (-(C)9 * cs2 * Q / (rho * rho * Rr));
         const C bPP = Q > (C)0 ? bQ / Q : (C)0;
-        const C bPxx = (C)2 * Pxx * bPP, bPyy = (C)2 * Pyy * bPP, bPzz = (C)2 * Pzz * bPP;
-        const C bPxy = (C)4 * Pxy * bPP, bPxz = (C)4 * Pxz * bPP, bPyz = (C)4 * Pyz * bPP;
-#pragma unroll
-        for (int q = 0; q < 19; ++q)
-          bneq[q] += (C)(cx(q) * cx(q)) * bPxx + (C)(cy(q) * cy(q)) * bPyy + (C)(cz(q) * cz(q)) * bPzz +
-                     (C)(cx(q) * cy(q)) * bPxy + (C)(cx(q) * cz(q)) * bPxz + (C)(cy(q) * cz(q)) * bPyz;
+        bPxx = (C)2 * Pxx * bPP;
+        bPyy = (C)2 * Pyy * bPP;
+        bPzz = (C)2 * Pzz * bPP;
+        bPxy = (C)4 * Pxy * bPP;
+        bPxz = (C)4 * Pxz * bPP;
+        bPyz = (C)4 * Pyz * bPP;
       }
-      // neq = f - feq: bar f = bar neq (already in bf), bar feq = lam* - bar neq
+      // bar f_eq = lam* - bar neq: its weighted moments D = omega L - moments of e^T bP e
+      // (D3Q19: sum w e_a^4 = 1/3, sum w e_a^2 e_b^2 = 1/9 for a != b, odd moments 0)
       {
+        WMom<C> D;
+        const C third = (C)1 / (C)3, ninth = (C)1 / (C)9;
+        D.m0 = omega * L.m0 - third * (bPxx + bPyy + bPzz);
+        D.x = omega * L.x;
+        D.y = omega * L.y;
+        D.z = omega * L.z;
+        D.xx = omega * L.xx - (third * bPxx + ninth * (bPyy + bPzz));
+        D.yy = omega * L.yy - (third * bPyy + ninth * (bPxx + bPzz));
+        D.zz = omega * L.zz - (third * bPzz + ninth * (bPxx + bPyy));
+        D.xy = omega * L.xy - ninth * bPxy;
+        D.xz = omega * L.xz - ninth * bPxz;
+        D.yz = omega * L.yz - ninth * bPyz;
         C br, bx, by, bz;
-        eq_vjp_diff<C>(ls, bneq, rho, ux, uy, uz, br, bx, by, bz);
+        eq_vjp<C>(D, rho, ux, uy, uz, br, bx, by, bz);
         brho += br;
         bux += bx;
         buy += by;
@@ -446,9 +469,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK, S == POG_STORE_F64 ? 1 : 2) adjoint
       bGz += (C)0.5 * bvz / rho;
       brho += -(bvx * vx + bvy * vy + bvz * vz) / rho;
       brho += bGx * (C)kp.gx + bGy * (C)kp.gy + bGz * (C)kp.gz;
+      const C keep = (C)1 - omega;
 #pragma unroll
       for (int q = 0; q < 19; ++q)
-        bf[q] += brho + (C)cx(q) * bmx + (C)cy(q) * bmy + (C)cz(q) * bmz;
+        bf[q] = keep * ls[q] + (C)(cx(q) * cx(q)) * bPxx + (C)(cy(q) * cy(q)) * bPyy +
+                (C)(cz(q) * cz(q)) * bPzz + (C)(cx(q) * cy(q)) * bPxy + (C)(cx(q) * cz(q)) * bPxz +
+                (C)(cy(q) * cz(q)) * bPyz + brho + (C)cx(q) * bmx + (C)cy(q) * bmy + (C)cz(q) * bmz;
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)bf[q];
@@ -517,15 +543,15 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
                       void* scratch, double* ge, double* gi, cudaStream_t s) {
   auto kern = adjoint_kernel<S>;
   static thread_local int grid = 0;
-  if (grid == 0) grid = persistent_blocks((const void*)kern, ADJ_BLOCK);
+  if (grid == 0) grid = persistent_blocks((const void*)kern, ADJ_STEP_BLOCK);
   if (grid <= 0) return set_error(POG_E_CUDA, "occupancy query failed");
-  int want = (int)((kp.n + ADJ_BLOCK - 1) / ADJ_BLOCK);
+  int want = (int)((kp.n + ADJ_STEP_BLOCK - 1) / ADJ_STEP_BLOCK);
   int g = want < grid ? want : grid;
   using E = typename Store<S>::E;
   using C = typename Store<S>::C;
   const uint32_t lo = (kp.nz - 2u) * kp.nxny, hi = lo + kp.nxny;  // the inlet plane
   C* bar_nu = scratch ? (C*)scratch : nullptr;
-  kern<<<g, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, pdrag, u_prev, (const E*)mu_in,
+  kern<<<g, ADJ_STEP_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, pdrag, u_prev, (const E*)mu_in,
                                bar_nu, ge, gi, lo, hi);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
