@@ -499,8 +499,11 @@ int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* 
  *   u_prev     [3][ncell] float, the velocity the forward step's stencil read (required)
  *   dJ_du      [3][ncell] (storage type) dJ/du_t of the velocity this step outputs, or NULL (0)
  *   dJ_du_prev [3][ncell] receives dJ/du_{t-1} (overwritten; required, != dJ_du)
- *   scratch    pog_adjoint_scratch_bytes(p) bytes of device memory (required)
- *   In the other LES modes these four are ignored (pass NULL).
+ *   In the other LES modes these three are ignored (pass NULL).
+ *   scratch   pog_adjoint_scratch_bytes(p) bytes of device memory, 16-byte aligned: required in
+ *             LES stencil mode; otherwise optional -- with it the inlet plane's dJ/da_k is summed
+ *             by many blocks (per-block sums added in block order), without it by one block;
+ *             either way in a fixed order, so gradients repeat bit for bit.
  *   The loss is J = sum_t flux_t with flux_t = POG_RED_OUTFLOW of step t, so each outlet
  *   cell adds dJ/df_i = -c_iz.  Parameter gradients are accumulated in FP64:
  *   grad_porosity [ncell] (nullable; needs porosity), grad_inlet [POG_INLET_NCOEF] (nullable).
@@ -510,7 +513,8 @@ int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next,
                      const uint32_t* flags, const float* porosity, const float* pdrag,
                      const float* u_prev, const void* dJ_du, void* dJ_du_prev, void* scratch,
                      double* grad_porosity, double* grad_inlet, void* stream);
-/* Scratch pog_adjoint_step needs in LES stencil mode (10 values per cell), 0 otherwise. */
+/* Scratch of pog_adjoint_step: 10 values per cell in LES stencil mode (rounded up to 16 bytes), then
+ * 16 doubles per 1,024 cells of an xy plane for the inlet plane's per-block sums. */
 size_t pog_adjoint_scratch_bytes(const pog_params* p);
 
 /* The outflow flux of a natural-layout state f_nat (F32 or F64 storage), flux = -sum over outlet

@@ -78,8 +78,9 @@ class OutflowAdjoint:
             self._uck = [torch.zeros_like(self._u) for _ in range(self.nseg)]
         if self.stencil:
             self._ups = [torch.zeros_like(self._u) for _ in range(self.K)]  # the segment's u_prev
-            self._scratch = torch.empty(int(self.lib.pog_adjoint_scratch_bytes(cfg.to_c())), dtype=torch.uint8,
-                                        device=self.device)
+        # the stencil mode's per-cell terms and the inlet plane's per-block gradient sums
+        self._scratch = torch.empty(int(self.lib.pog_adjoint_scratch_bytes(cfg.to_c())), dtype=torch.uint8,
+                                    device=self.device)
         if particles is not None:
             self._init_particles(particles)
 
@@ -200,8 +201,35 @@ class OutflowAdjoint:
         hi, lo = (int(v) for v in self._jfix.tolist())
         return float(hi) * 2.0 ** -48 + float(lo) * 2.0 ** -96
 
-    def backward(self, want_porosity_grad: bool = True) -> AdjointResult:
+    def _segment(self, n, lam_next, lam_t, mu, mu_prev, g_eps, g_in):
+        """Recompute n states from self._states[0] (and the velocity / particles restored beside
+        it), then run the adjoint back through them.  Returns the ping-pong buffers as they stand
+        after the n adjoint steps."""
         s = _lib.stream_handle()
+        for i in range(n):
+            if self.stencil:
+                self._ups[i].copy_(self._u)
+            if self.pc is not None:
+                self._couple(self._u, self._deps[i])
+            if i + 1 < n:
+                self._push(self._states[i], self._states[i + 1], self._deps[i] if self.pc is not None else None)
+        for i in reversed(range(n)):
+            dep = self._deps[i] if self.pc is not None else None
+            _lib.check(self.lib.pog_adjoint_step(
+                self._p, _lib.ptr(self._states[i]), _lib.ptr(lam_next), _lib.ptr(lam_t),
+                _lib.ptr(self.flags), _lib.ptr(self._eps), _lib.ptr(dep),
+                _lib.ptr(self._ups[i]) if self.stencil else None, _lib.ptr(mu), _lib.ptr(mu_prev),
+                _lib.ptr(self._scratch), _lib.ptr(g_eps), _lib.ptr(g_in), s))
+            lam_next, lam_t = lam_t, lam_next
+            if self.stencil:
+                mu, mu_prev = mu_prev, mu
+        return lam_next, lam_t, mu, mu_prev
+
+    def backward(self, want_porosity_grad: bool = True, graphs: bool = True) -> AdjointResult:
+        """Segments last first.  With `graphs`, a full segment (K steps) is captured into a CUDA
+        graph once per backward pass (after one segment has run eagerly) and replayed for the
+        others: the same launches on the same buffers, so the gradients are bit-identical to the
+        eager pass; the segment's restore copies stay outside the graph."""
         lam_next = torch.zeros((19,) + self.shape, dtype=self.dtype, device=self.device)
         lam_t = torch.zeros_like(lam_next)
         g_eps = torch.zeros(self.shape, dtype=torch.float64, device=self.device) \
@@ -212,9 +240,14 @@ class OutflowAdjoint:
         if self.stencil:
             mu = torch.zeros((3,) + self.shape, dtype=self.dtype, device=self.device)
             mu_prev = torch.zeros_like(mu)
+        u_pair = (self._u, self._un) if self._need_u else None
+        captured = {}  # (lam_next, mu) buffer identity at segment start -> (graph, buffers after it)
+        warm = False
         for seg in reversed(range(self.nseg)):
             t0 = seg * self.K
-            t1 = min(self.T, t0 + self.K)
+            n = min(self.T, t0 + self.K) - t0
+            if u_pair is not None:  # the same velocity buffers at every segment start
+                self._u, self._un = u_pair
             self._states[0].copy_(self._ckpt[seg])
             # recompute the segment: the same states, velocities and deposits as the forward pass
             if self._need_u:
@@ -222,23 +255,23 @@ class OutflowAdjoint:
             if self.pc is not None:
                 for a, b in zip(self._part, self._pck[seg]):
                     a.copy_(b)
-            for i in range(t1 - t0):
-                if self.stencil:
-                    self._ups[i].copy_(self._u)
-                if self.pc is not None:
-                    self._couple(self._u, self._deps[i])
-                if i + 1 < t1 - t0:
-                    self._push(self._states[i], self._states[i + 1], self._deps[i] if self.pc is not None else None)
-            for t in reversed(range(t0, t1)):
-                dep = self._deps[t - t0] if self.pc is not None else None
-                _lib.check(self.lib.pog_adjoint_step(
-                    self._p, _lib.ptr(self._states[t - t0]), _lib.ptr(lam_next), _lib.ptr(lam_t),
-                    _lib.ptr(self.flags), _lib.ptr(self._eps), _lib.ptr(dep),
-                    _lib.ptr(self._ups[t - t0]) if self.stencil else None, _lib.ptr(mu), _lib.ptr(mu_prev),
-                    _lib.ptr(self._scratch) if self.stencil else None, _lib.ptr(g_eps), _lib.ptr(g_in), s))
-                lam_next, lam_t = lam_t, lam_next
-                if self.stencil:
-                    mu, mu_prev = mu_prev, mu
+            key = (lam_next.data_ptr(), mu.data_ptr() if mu is not None else 0)
+            if graphs and warm and n == self.K and key not in captured:
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    out = self._segment(n, lam_next, lam_t, mu, mu_prev, g_eps, g_in)
+                captured[key] = (g, out, (self._u, self._un) if self._need_u else None)
+            if key in captured and n == self.K:
+                g, out, u_end = captured[key]
+                g.replay()
+                lam_next, lam_t, mu, mu_prev = out
+                if u_end is not None:
+                    self._u, self._un = u_end
+            else:
+                lam_next, lam_t, mu, mu_prev = self._segment(n, lam_next, lam_t, mu, mu_prev, g_eps, g_in)
+                warm = True
+        if u_pair is not None:
+            self._u, self._un = u_pair
         return AdjointResult(self._loss(), g_eps, g_in)
 
     def loss(self, porosity: Optional[torch.Tensor], inlet_coef) -> float:

@@ -124,22 +124,27 @@ __device__ __forceinline__ void adj_pull(const KParams& kp, const typename Store
   }
 }
 
-// The inlet disk's plane (k = nz - 2, where pog_build_flags puts the inlet): one block, so the
-// dJ/da_k sums have a fixed order and repeat bit for bit.
+// The inlet disk's plane (k = nz - 2, where pog_build_flags puts the inlet).  Block b takes the
+// cells [lo + b chunk, lo + (b + 1) chunk) and sums its cells' dJ/da_k in a fixed order (thread
+// partials, warp shuffles, then the warps in order); with `part` it writes the block's 16 sums to
+// part[b] for inlet_sum_kernel, without it (one block over the whole plane) it adds them to
+// grad_inlet itself.  Either way the gradients repeat bit for bit.
 template <int S>
 __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
     const KParams kp, const typename Store<S>::E* __restrict__ ft,
     const typename Store<S>::E* __restrict__ lam_next, typename Store<S>::E* __restrict__ lam_t,
-    const uint32_t* __restrict__ flags, uint32_t lo, uint32_t hi, const typename Store<S>::E* __restrict__ mu_in,
-    double* __restrict__ grad_inlet) {
+    const uint32_t* __restrict__ flags, uint32_t lo, uint32_t hi, uint32_t chunk,
+    const typename Store<S>::E* __restrict__ mu_in, double* __restrict__ part, double* __restrict__ grad_inlet) {
   using St = Store<S>;
   using C = typename St::C;
   using E = typename St::E;
   const uint32_t n = kp.n;
+  const uint32_t b0 = lo + blockIdx.x * chunk;
+  const uint32_t b1 = hi - b0 < chunk ? hi : b0 + chunk;
   double g[POG_INLET_NCOEF];
 #pragma unroll
   for (int k = 0; k < POG_INLET_NCOEF; ++k) g[k] = 0.0;
-  for (uint32_t c = lo + threadIdx.x; c < hi; c += ADJ_BLOCK) {
+  for (uint32_t c = b0 + threadIdx.x; c < b1; c += ADJ_BLOCK) {
     const uint32_t fl = flags[c];
     if (!(fl & POG_CELL_INLET) || (fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
     C ls[19];
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
 #pragma unroll
     for (int q = 0; q < 19; ++q) lam_t[(uint32_t)q * n + c] = (E)brho;
   }
-  if (!grad_inlet) return;
+  if (!part && !grad_inlet) return;
   __shared__ double sm[POG_INLET_NCOEF][ADJ_BLOCK / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -165,9 +170,24 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
   if (threadIdx.x < POG_INLET_NCOEF) {
     double x = 0.0;
     for (int w = 0; w < ADJ_BLOCK / 32; ++w) x += sm[threadIdx.x][w];
-    grad_inlet[threadIdx.x] += x;
+    if (part)
+      part[(size_t)blockIdx.x * POG_INLET_NCOEF + threadIdx.x] = x;
+    else
+      grad_inlet[threadIdx.x] += x;
   }
 }
+
+// grad_inlet[k] += sum over blocks b (in order) of part[b][k].
+__global__ void inlet_sum_kernel(const double* __restrict__ part, uint32_t nblocks, double* __restrict__ grad_inlet) {
+  const uint32_t k = threadIdx.x;
+  if (k >= POG_INLET_NCOEF) return;
+  double x = 0.0;
+  for (uint32_t b = 0; b < nblocks; ++b) x += part[(size_t)b * POG_INLET_NCOEF + k];
+  grad_inlet[k] += x;
+}
+
+// Cells of the inlet plane per block of the parallel inlet pass: four per thread.
+constexpr uint32_t INLET_CHUNK = 4u * ADJ_BLOCK;
 
 template <int S>
 __global__ void __launch_bounds__(ADJ_STEP_BLOCK, (adj_min_blocks<S>())) adjoint_kernel(
@@ -537,6 +557,12 @@ __global__ void les_mu_kernel(const KParams kp, const C* __restrict__ bar_g, E* 
   }
 }
 
+// Bytes of the stencil mode's part of the adjoint scratch (bar_nu and bar_g, 10 values per cell),
+// rounded up to 16 bytes; the inlet pass's per-block sums follow.
+static inline size_t adj_stencil_bytes(size_t n, bool stencil, size_t elem) {
+  return stencil ? (10 * n * elem + 15) / 16 * 16 : 0;
+}
+
 template <int S>
 static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* lt, const uint32_t* flags,
                       const float* eps, const float* pdrag, const float* u_prev, const void* mu_in, void* mu_out,
@@ -550,16 +576,33 @@ static int launch_adj(const KParams& kp, const void* ft, const void* ln, void* l
   using E = typename Store<S>::E;
   using C = typename Store<S>::C;
   const uint32_t lo = (kp.nz - 2u) * kp.nxny, hi = lo + kp.nxny;  // the inlet plane
-  C* bar_nu = scratch ? (C*)scratch : nullptr;
+  const bool stencil = kp.les_mode == POG_LES_STENCIL;
+  // scratch: the stencil mode's bar_nu [n] and bar_g [9 n] (storage type), then the inlet pass's
+  // per-block sums (pog_adjoint_scratch_bytes)
+  C* bar_nu = (scratch && stencil) ? (C*)scratch : nullptr;
+  double* part = scratch ? (double*)((char*)scratch + adj_stencil_bytes(kp.n, stencil, sizeof(C))) : nullptr;
   kern<<<g, ADJ_STEP_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, eps, pdrag, u_prev, (const E*)mu_in,
                                bar_nu, ge, gi, lo, hi);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
-  adjoint_inlet_kernel<S><<<1, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi,
-                                                  (const E*)mu_in, gi);
-  count_launch();
-  POG_TRY_CUDA(cudaGetLastError());
-  if (scratch && mu_out) {
+  if (part) {
+    const uint32_t nb = (kp.nxny + INLET_CHUNK - 1) / INLET_CHUNK;
+    adjoint_inlet_kernel<S><<<nb, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi,
+                                                     INLET_CHUNK, (const E*)mu_in, gi ? part : nullptr, nullptr);
+    count_launch();
+    POG_TRY_CUDA(cudaGetLastError());
+    if (gi) {
+      inlet_sum_kernel<<<1, 32, 0, s>>>(part, nb, gi);
+      count_launch();
+      POG_TRY_CUDA(cudaGetLastError());
+    }
+  } else {
+    adjoint_inlet_kernel<S><<<1, ADJ_BLOCK, 0, s>>>(kp, (const E*)ft, (const E*)ln, (E*)lt, flags, lo, hi,
+                                                    kp.nxny, (const E*)mu_in, nullptr, gi);
+    count_launch();
+    POG_TRY_CUDA(cudaGetLastError());
+  }
+  if (bar_nu && mu_out) {
     C* bar_g = bar_nu + kp.n;
     les_grad_vjp_kernel<C><<<g, ADJ_BLOCK, 0, s>>>(kp, u_prev, bar_nu, bar_g);
     les_mu_kernel<C, E><<<g, ADJ_BLOCK, 0, s>>>(kp, bar_g, (E*)mu_out);
@@ -626,9 +669,11 @@ extern "C" int pog_outflow_fixed(const pog_params* p, const void* f_nat, const u
 }
 
 extern "C" size_t pog_adjoint_scratch_bytes(const pog_params* p) {
-  if (!p || p->les_mode != POG_LES_STENCIL) return 0;
-  const size_t n = (size_t)p->nx * p->ny * p->nz;
-  return 10 * n * (p->storage == POG_STORE_F64 ? sizeof(double) : sizeof(float));
+  if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0) return 0;
+  const size_t n = (size_t)p->nx * p->ny * p->nz, nxny = (size_t)p->nx * p->ny;
+  const size_t elem = p->storage == POG_STORE_F64 ? sizeof(double) : sizeof(float);
+  const size_t nb = (nxny + INLET_CHUNK - 1) / INLET_CHUNK;
+  return adj_stencil_bytes(n, p->les_mode == POG_LES_STENCIL, elem) + nb * POG_INLET_NCOEF * sizeof(double);
 }
 
 extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void* lam_next,
@@ -643,12 +688,12 @@ extern "C" int pog_adjoint_step(const pog_params* p, const void* f_t, const void
   if (stencil && (!u_prev || !dJ_du_prev || !scratch))
     return set_error(POG_E_ARG, "LES stencil mode needs u_prev, dJ_du_prev and scratch");
   if (stencil && dJ_du == dJ_du_prev) return set_error(POG_E_ARG, "dJ_du and dJ_du_prev must differ");
-  if (!stencil) {
+  if (!stencil) {  // scratch stays: the inlet pass's per-block sums
     u_prev = nullptr;
     dJ_du = nullptr;
     dJ_du_prev = nullptr;
-    scratch = nullptr;
   }
+  if (scratch && ((uintptr_t)scratch & 15u)) return set_error(POG_E_ARG, "scratch must be 16-byte aligned");
   if (p->drag_mode != POG_DRAG_SEMI_IMPLICIT || p->forcing_mode != POG_FORCING_GUO || p->clamp_tau)
     return set_error(POG_E_ARG, "adjoint supports semi-implicit drag, Guo forcing, no tau clamp");
   if (grad_porosity && !porosity) return set_error(POG_E_ARG, "grad_porosity needs porosity");

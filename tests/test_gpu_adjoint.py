@@ -280,3 +280,53 @@ def test_loss_repeats_bit_for_bit(cuda):
     run = OutflowAdjoint(cfg, steps=30, checkpoint_every=10)
     js = {run.forward(None, cfg.inlet_coef) for _ in range(3)}
     assert len(js) == 1 and next(iter(js)) != 0.0
+
+
+@pytest.mark.parametrize("mode", ["plain_f32", "stencil", "coupled"])
+def test_graph_replayed_segments_equal_eager(cuda, mode):
+    """backward() replays full checkpoint segments as captured CUDA graphs (one capture per
+    ping-pong parity, after one eager segment); the same launches on the same buffers give the
+    eager pass's gradients bit for bit.  K = 5 (odd) makes the adjoint buffers alternate between
+    segments, so two graphs are captured; the stencil case carries the velocity adjoint too."""
+    pc = None
+    if mode == "coupled":
+        cfg, pc = _coupled_case()
+    elif mode == "stencil":
+        cfg = _stencil_case()
+    else:
+        cfg = _case().replace(storage=STORE_F32, nx=20, ny=20, nz=24, cone_apex_z=3.0, inlet_radius=5.0)
+    from gpu_helpers import gpu_flags
+    fl = gpu_flags(cfg).cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=9)).reshape(cfg.nz, cfg.ny, cfg.nx)
+    run = OutflowAdjoint(cfg, steps=22, checkpoint_every=5, particles=pc)
+    run.forward(eps, cfg.inlet_coef)
+    ra = run.backward(graphs=False)
+    rb = run.backward(graphs=True)
+    assert torch.equal(ra.grad_inlet, rb.grad_inlet) and torch.equal(ra.grad_porosity, rb.grad_porosity)
+    assert rb.grad_porosity.abs().max() > 0
+
+
+def test_inlet_gradient_with_and_without_scratch(cuda):
+    """pog_adjoint_step sums the inlet plane's dJ/da_k by many blocks when given scratch (per-block
+    sums added in block order) and by one block without it: the same lam_t bit for bit, the same
+    gradients to FP64 rounding, and each form repeats itself bit for bit."""
+    from pour_over_coffee_lbm_gb300 import _lib
+    cfg = _case().replace(storage=STORE_F64, nx=40, ny=40, nz=24, cone_apex_z=3.0, inlet_radius=14.0)
+    run = OutflowAdjoint(cfg, steps=4, checkpoint_every=4)
+    run.forward(None, cfg.inlet_coef)
+    torch.manual_seed(3)
+    lam = torch.randn((19,) + run.shape, dtype=torch.float64, device="cuda")
+    outs = []
+    for scratch in (run._scratch, None, run._scratch, None):
+        lt = torch.empty_like(lam)
+        gi = torch.zeros(16, dtype=torch.float64, device="cuda")
+        _lib.check(run.lib.pog_adjoint_step(run._p, _lib.ptr(run._states[2]), _lib.ptr(lam), _lib.ptr(lt),
+                                            _lib.ptr(run.flags), None, None, None, None, None, _lib.ptr(scratch),
+                                            None, _lib.ptr(gi), _lib.stream_handle()))
+        outs.append((lt, gi))
+    torch.cuda.synchronize()
+    (la, ga), (lb, gb), (lc, gc), (ld, gd) = outs
+    assert torch.equal(la, lb) and torch.equal(la, lc) and torch.equal(la, ld)
+    assert torch.equal(ga, gc) and torch.equal(gb, gd)
+    assert ga.abs().max() > 0
+    assert torch.allclose(ga, gb, rtol=1e-12, atol=1e-15 * gb.abs().max().item())
