@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--precision-case", choices=["les_band", "plain"], default="les_band")
     ap.add_argument("--coupled-only", action="store_true",
                     help="print only the coupled 128^3 / 20,000-particle line (profiling)")
+    ap.add_argument("--adjoint-only", type=int, default=0, metavar="N",
+                    help="time the adjoint step kernel alone on an N^3 FP32 LES + band lattice")
     ap.add_argument("--scale-only", action="store_true",
                     help="run --steps coupled steps of the 320x320x384 / 1M-particle case (profiling)")
     ap.add_argument("--step-kernel", choices=["auto", "rows", "registers"], default="auto",
@@ -1003,9 +1005,63 @@ def run_coupled_only(args):
     print(json.dumps({"coupled_only": coupled_line(args, peaks())}), flush=True)
 
 
+def run_adjoint_only(args):
+    """The adjoint step (pog_adjoint_step: adjoint_kernel + the inlet-plane pass) alone on an N^3
+    FP32 LES(local) + porous-band lattice with a porosity field, on a recomputed forward state:
+    `--steps` calls timed with CUDA events after 3 warm-up calls.  Algorithmic bytes per call:
+    232 B per non-solid cell (f_t, lam_{t+1} and lam_t, 19 x 4 B each, and the flag word), 80 B
+    per solid cell (flag word, lam_t zeroed), and 20 B more per porous cell (porosity, the FP64
+    porosity gradient read and written)."""
+    import torch
+    from pour_over_coffee_lbm_gb300 import _lib
+    from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint
+    from pour_over_coffee_lbm_gb300.params import CELL_POROUS, CELL_SOLID, LES_LOCAL, STORE_F32, LatticeConfig, \
+        porosity_field
+    torch.cuda.set_device(0)
+    N = args.adjoint_only
+    cfg = LatticeConfig(nx=N, ny=N, nz=N, band_thickness=3.0, les_mode=LES_LOCAL, storage=STORE_F32, u_inlet=-0.05)
+    run = OutflowAdjoint(cfg, 8, 4)
+    fl = run.flags.cpu().numpy()
+    eps = torch.as_tensor(porosity_field(cfg, fl, seed=1234)).reshape(cfg.nz, cfg.ny, cfg.nx).cuda()
+    run.forward(eps, cfg.inlet_coef)
+    run.backward()
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    lam = torch.randn((19,) + run.shape, device="cuda", generator=gen) * 1e-3
+    lam_t = torch.zeros_like(lam)
+    g_eps = torch.zeros(run.shape, dtype=torch.float64, device="cuda")
+    g_in = torch.zeros(16, dtype=torch.float64, device="cuda")
+    s = _lib.stream_handle()
+
+    def call():
+        _lib.check(run.lib.pog_adjoint_step(run._p, _lib.ptr(run._states[1]), _lib.ptr(lam), _lib.ptr(lam_t),
+                                            _lib.ptr(run.flags), _lib.ptr(run._eps), None, None, None, None,
+                                            _lib.ptr(run._scratch), _lib.ptr(g_eps), _lib.ptr(g_in), s))
+    for _ in range(3):
+        call()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    for _ in range(args.steps):
+        call()
+    ev[1].record()
+    torch.cuda.synchronize()
+    us = ev[0].elapsed_time(ev[1]) * 1e3 / args.steps
+    solid = int(((run.flags & CELL_SOLID) != 0).sum().item())
+    porous = int((((run.flags & CELL_POROUS) != 0) & ((run.flags & CELL_SOLID) == 0)).sum().item())
+    nbytes = 232 * (cfg.ncell - solid) + 80 * solid + 20 * porous
+    peak = peaks()
+    gbs = nbytes / us / 1e3
+    print(json.dumps({"adjoint_only": N, "calls": args.steps, "us_per_call": round(us, 1),
+                      "mlups": round(cfg.ncell / us, 1), "algorithmic_bytes": nbytes, "achieved_gbs": round(gbs, 1),
+                      "frac": round(gbs / peak[0], 4), "peak_source": peak[1],
+                      "finite": bool(torch.isfinite(lam_t).all())}), flush=True)
+
+
 def main():
     args = parse()
-    if args.precision_only:
+    if args.adjoint_only:
+        run_adjoint_only(args)
+    elif args.precision_only:
         run_precision_only(args)
     elif args.coupled_only:
         run_coupled_only(args)

@@ -25,12 +25,12 @@
 namespace pog {
 
 constexpr int ADJ_BLOCK = 256;
-// The adjoint step kernel: 128-thread blocks, 5 resident per SM for FP32 (96 registers, no spill:
-// 20 warps per SM against 16 at 256 x 2 and 128 registers), FP64 at its register need (221).
+// The adjoint step kernel: 128-thread blocks, 4 resident per SM for FP32 (128 registers, no spill;
+// at 96 registers and 5 blocks it spills 60 bytes and runs 3 % slower), FP64 at its register need.
 constexpr int ADJ_STEP_BLOCK = 128;
 template <int S>
 constexpr int adj_min_blocks() {
-  return S == POG_STORE_F64 ? 1 : 5;
+  return S == POG_STORE_F64 ? 1 : 4;
 }
 
 // Weighted lattice moments of a direction vector a_q: m0 = sum w_q a_q, m1_a = sum w_q a_q e_qa,
@@ -110,17 +110,23 @@ __device__ __forceinline__ C adj_inlet_cell(const KParams& kp, uint32_t c, const
   return brho;
 }
 
-// The pull of the transposed streaming and the density of cell c (shared by both kernels).
+// The pull of the transposed streaming at cell c: lam*_q = lam_{t+1} at slot (c + e_q, q), element
+// c + wr[q], or lam_{t+1} at (c, opp q), element c + pl[opp q], when c + e_q is solid.  `open`
+// (warp-uniform: no cell of the warp has a solid neighbour) skips the per-direction choice.
 template <int S>
 __device__ __forceinline__ void adj_pull(const KParams& kp, const typename Store<S>::E* __restrict__ lam_next,
-                                         uint32_t c, uint32_t fl, typename Store<S>::C ls[19]) {
+                                         uint32_t c, uint32_t fl, bool open, typename Store<S>::C ls[19]) {
   using C = typename Store<S>::C;
-  const uint32_t n = kp.n;
+  const typename Store<S>::E* __restrict__ lc = lam_next + c;
+  if (open) {
 #pragma unroll
-  for (int q = 0; q < 19; ++q) {
-    const uint32_t dst = c + (uint32_t)kp.off[q];
-    const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
-    ls[q] = wall ? (C)lam_next[(uint32_t)opp(q) * n + c] : (C)lam_next[(uint32_t)q * n + dst];
+    for (int q = 0; q < 19; ++q) ls[q] = (C)lc[kp.wr[q]];
+  } else {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+      const bool wall = q != 0 && ((fl >> (POG_LINK_SHIFT + q)) & 1u);
+      ls[q] = (C)lc[wall ? kp.pl[opp(q)] : kp.wr[q]];
+    }
   }
 }
 
@@ -148,7 +154,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_inlet_kernel(
     const uint32_t fl = flags[c];
     if (!(fl & POG_CELL_INLET) || (fl & POG_CELL_SOLID) || c < kp.guard_lo || c > kp.guard_hi) continue;
     C ls[19];
-    adj_pull<S>(kp, lam_next, c, fl, ls);
+    adj_pull<S>(kp, lam_next, c, fl, false, ls);
     C rho = 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) rho += St::ld(ft, (uint32_t)q * n + c, q, (C)kp.rho0);
@@ -220,19 +226,27 @@ __global__ void __launch_bounds__(ADJ_STEP_BLOCK, (adj_min_blocks<S>())) adjoint
     if ((fl & POG_CELL_INLET) && c >= inlet_lo && c < inlet_hi) continue;
     // 1. transpose of push streaming
     C ls[19];
-    adj_pull<S>(kp, lam_next, c, fl, ls);
-    C f[19];
-    const C rs = (C)kp.rho0;
-#pragma unroll
-    for (int q = 0; q < 19; ++q) f[q] = St::ld(ft, (uint32_t)q * n + c, q, rs);
-    C rho = 0, mx = 0, my = 0, mz = 0;
+    const bool open = __all_sync(__activemask(), (fl >> POG_LINK_SHIFT) == 0u);
+    adj_pull<S>(kp, lam_next, c, fl, open, ls);
+    // the stored deviations h_q = f_q - w_q rho0: density deviation, momentum, raw second moments
+    // and sum_q lam*_q h_q in one pass (f itself is never formed; no O(1) terms cancel)
+    C drho = 0, mx = 0, my = 0, mz = 0, Sxx = 0, Syy = 0, Szz = 0, Sxy = 0, Sxz = 0, Syz = 0, lh = 0;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-      rho += f[q];
-      mx += (C)cx(q) * f[q];
-      my += (C)cy(q) * f[q];
-      mz += (C)cz(q) * f[q];
+      const C h = St::dech(ft[(uint32_t)q * n + c]);
+      drho += h;
+      if (cx(q)) mx += (C)cx(q) * h;
+      if (cy(q)) my += (C)cy(q) * h;
+      if (cz(q)) mz += (C)cz(q) * h;
+      if (cx(q)) Sxx += h;
+      if (cy(q)) Syy += h;
+      if (cz(q)) Szz += h;
+      if (cx(q) && cy(q)) Sxy += (C)(cx(q) * cy(q)) * h;
+      if (cx(q) && cz(q)) Sxz += (C)(cx(q) * cz(q)) * h;
+      if (cy(q) && cz(q)) Syz += (C)(cy(q) * cz(q)) * h;
+      lh += ls[q] * h;
     }
+    const C rho = (C)kp.rho0 + drho;
     C brho = 0, bmx = 0, bmy = 0, bmz = 0;
     C bf[19];
     if (fl & POG_CELL_INLET) {
@@ -306,13 +320,6 @@ __global__ void __launch_bounds__(ADJ_STEP_BLOCK, (adj_min_blocks<S>())) adjoint
         Fy = Gy + Kvy - (coef + Kp) * uy;
         Fz = Gz + Kvz - (coef + Kp) * uz;
       }
-      // f becomes f - f_eq in place (f itself is not needed again)
-      C* const neq = f;
-      {
-        const C usq15 = (C)1.5 * (ux * ux + uy * uy + uz * uz);
-#pragma unroll
-        for (int q = 0; q < 19; ++q) neq[q] = f[q] - feq_q<C>(q, rho, ux, uy, uz, usq15);
-      }
       const C tau0 = (C)kp.tau;
       C tau = tau0;
       bool les_live = false;
@@ -329,16 +336,15 @@ __global__ void __launch_bounds__(ADJ_STEP_BLOCK, (adj_min_blocks<S>())) adjoint
       }
       C Pxx = 0, Pyy = 0, Pzz = 0, Pxy = 0, Pxz = 0, Pyz = 0, Q = 0, Rr = 0;
       if (kp.les_mode == POG_LES_LOCAL && !porous) {
-#pragma unroll
-        for (int q = 0; q < 19; ++q) {
-          const C d = neq[q];
-          Pxx += (C)(cx(q) * cx(q)) * d;
-          Pyy += (C)(cy(q) * cy(q)) * d;
-          Pzz += (C)(cz(q) * cz(q)) * d;
-          Pxy += (C)(cx(q) * cy(q)) * d;
-          Pxz += (C)(cx(q) * cz(q)) * d;
-          Pyz += (C)(cy(q) * cz(q)) * d;
-        }
+        // Pi_neq = sum e e (f - f_eq) = S(h) - (drho / 3) I - rho u u (the D3Q19 equilibrium's
+        // second moment is rho / 3 I + rho u u)
+        const C d3 = drho * ((C)1 / (C)3);
+        Pxx = Sxx - d3 - rho * ux * ux;
+        Pyy = Syy - d3 - rho * uy * uy;
+        Pzz = Szz - d3 - rho * uz * uz;
+        Pxy = Sxy - rho * ux * uy;
+        Pxz = Sxz - rho * ux * uz;
+        Pyz = Syz - rho * uy * uz;
         const C PP = Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + (C)2 * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz);
         Q = sqrt((C)2 * PP);
         Rr = sqrt(tau0 * tau0 + (C)18 * (C)kp.cs2 * Q / rho);
@@ -362,13 +368,14 @@ __global__ void __launch_bounds__(ADJ_STEP_BLOCK, (adj_min_blocks<S>())) adjoint
       // ---- reverse ----
       // f* = f_eq + (1 - omega) neq + A w_q B_q, neq = f - f_eq.  Every sum over q below is a
       // contraction of the weighted moments L of lam* (the sums of w lam* times 1, e_a, e_a e_b).
-      C bomega = 0;
-#pragma unroll
-      for (int q = 0; q < 19; ++q) bomega -= ls[q] * neq[q];
       const WMom<C> L = wmoments<C>(ls);
-      // the forcing term S_q = A w_q B_q, B_q = 3 (e.F - u.F) + 9 (e.u)(e.F)
       const C L2ux = L.xx * ux + L.xy * uy + L.xz * uz, L2uy = L.xy * ux + L.yy * uy + L.yz * uz,
               L2uz = L.xz * ux + L.yz * uy + L.zz * uz;
+      // bar omega = -sum lam* neq = -sum lam* h - rho0 L0 + sum lam* f_eq
+      const C usq = ux * ux + uy * uy + uz * uz;
+      C bomega = -lh + L.m0 * (drho - (C)1.5 * rho * usq) +
+                 rho * ((C)3 * (ux * L.x + uy * L.y + uz * L.z) + (C)4.5 * (ux * L2ux + uy * L2uy + uz * L2uz));
+      // the forcing term S_q = A w_q B_q, B_q = 3 (e.F - u.F) + 9 (e.u)(e.F)
       const C L2Fx = L.xx * Fx + L.xy * Fy + L.xz * Fz, L2Fy = L.xy * Fx + L.yy * Fy + L.yz * Fz,
               L2Fz = L.xz * Fx + L.yz * Fy + L.zz * Fz;
       const C bA = (C)3 * (Fx * L.x + Fy * L.y + Fz * L.z - uF * L.m0) +
