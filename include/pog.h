@@ -486,6 +486,15 @@ int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cell
 /* pdrag[a][c] = pdrag_fix[a][c] * 2^-32, a = 0..3 (deterministic-mode conversion). */
 int pog_drag_from_fixed(const pog_params* p, const long long* pdrag_fix, float* pdrag,
                         void* stream);
+/* The same conversion at the deposit cells of the np particles only (deposit_cells from the
+ * pog_particles_couple pass that filled pdrag_fix; order nullable, as in
+ * pog_particles_clear_deposit): pdrag[a][c] += pdrag_fix[a][c] * 2^-32 at each cell a particle
+ * deposited on, and those pdrag_fix entries -- all its nonzero ones -- are zeroed, each entry
+ * taken once however many particles share the cell.  pdrag_fix is therefore all zeros again for
+ * the next pass, and pdrag equals pog_drag_from_fixed's field added to it, at the cost of the
+ * particles' cells rather than of two full-field passes. */
+int pog_drag_from_fixed_cells(const pog_params* p, long long* pdrag_fix, const int32_t* deposit_cells, int np,
+                              const int32_t* order, float* pdrag, void* stream);
 
 /* ---- adjoint --------------------------------------------------------------------------------- */
 /* Reverse of one pog_step_push step (natural layout, storage F32 or F64).

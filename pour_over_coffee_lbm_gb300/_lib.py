@@ -53,6 +53,7 @@ SIGNATURES = [
     ("pog_particles_clear_deposit", _i, [_P, _v, _i, _v, _v, _v, _v]),
     ("pog_zero", _i, [_v, ctypes.c_size_t, _v]),
     ("pog_drag_from_fixed", _i, [_P, _v, _v, _v]),
+    ("pog_drag_from_fixed_cells", _i, [_P, _v, _v, _i, _v, _v, _v]),
     ("pog_adjoint_step", _i, [_P, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _v]),
     ("pog_adjoint_scratch_bytes", ctypes.c_size_t, [_P]),
     ("pog_device_status", _i, [_i]),

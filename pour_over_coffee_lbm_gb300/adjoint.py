@@ -99,18 +99,23 @@ class OutflowAdjoint:
         self._part = [a.clone() for a in self._p0]  # pos, vel, drag_old, active
         self._pck = [[a.clone() for a in self._p0] for _ in range(self.nseg)]
         n = self.cfg.ncell
+        # the fixed-point deposit: all zeros between passes (each pass's conversion takes back
+        # every entry it deposited); the base cell of each particle's deposit
         self._fix = torch.zeros(4 * n, dtype=torch.int64, device=dev)
+        self._depc = torch.full((pc.count,), -1, dtype=torch.int32, device=dev)
+        self._pp.deposit_cells = self._depc.data_ptr()
         self._deps = [torch.zeros((4,) + self.shape, dtype=torch.float32, device=dev) for _ in range(self.K)]
         self._dep_hist = None  # all T deposits of the last forward (for loss_frozen), on request
 
     def _couple(self, u, out):
         """One coupling pass on the current particle state in velocity u; deposit into out."""
         pos, vel, drag, act = self._part
-        self._fix.zero_()
+        out.zero_()
         _lib.check(self.lib.pog_particles_couple(self._p, self._pp, _lib.ptr(pos), _lib.ptr(vel), _lib.ptr(self._d),
                                                  _lib.ptr(drag), _lib.ptr(act), int(self.pc.count), None,
                                                  _lib.ptr(u), None, _lib.ptr(self._fix), None, _lib.stream_handle()))
-        _lib.check(self.lib.pog_drag_from_fixed(self._p, _lib.ptr(self._fix), _lib.ptr(out), _lib.stream_handle()))
+        _lib.check(self.lib.pog_drag_from_fixed_cells(self._p, _lib.ptr(self._fix), _lib.ptr(self._depc),
+                                                      int(self.pc.count), None, _lib.ptr(out), _lib.stream_handle()))
 
     # ---- steps ---------------------------------------------------------------------------------
     def _params(self, coef):

@@ -473,6 +473,31 @@ __global__ void clear_deposit_kernel(uint32_t n, uint32_t sy, uint32_t sz, const
     for (int cc = 0; cc < 8; ++cc) pdrag[(size_t)a * n + nodes[cc]] = 0.0f;
 }
 
+// The deterministic deposit converted at the particles' cells only: each particle with a deposit
+// takes the 4 fixed-point entries of its 8 corner cells, each by an atomic exchange with 0, so an
+// entry shared by several particles is converted once (by whichever takes it first) and the
+// fixed-point field is all zeros afterwards; the value added to pdrag is the one
+// fixed_to_float_kernel computes.
+__global__ void fixed_to_float_cells_kernel(uint32_t n, uint32_t sy, uint32_t sz, const int32_t* __restrict__ dep,
+                                            const int32_t* __restrict__ order, int np,
+                                            unsigned long long* __restrict__ fix, float* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= np) return;
+  const int32_t c = dep[order ? order[t] : t];
+  if (c < 0) return;
+  const uint32_t c0 = (uint32_t)c;
+  const uint32_t nodes[8] = {c0, c0 + sz, c0 + sy, c0 + sy + sz, c0 + 1, c0 + 1 + sz, c0 + 1 + sy, c0 + 1 + sy + sz};
+  const double inv = 1.0 / FIX_SCALE;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) {
+      const size_t i = (size_t)a * n + nodes[cc];
+      const unsigned long long v = atomicExch(fix + i, 0ull);
+      if (v != 0ull) out[i] += (float)((double)(long long)v * inv);
+    }
+}
+
 __global__ void fixed_to_float_kernel(uint32_t n3, const long long* __restrict__ fix,
                                       float* __restrict__ out) {
   const double inv = 1.0 / FIX_SCALE;
@@ -633,6 +658,21 @@ int pog_particles_clear_deposit(const pog_params* p, const int32_t* deposit_cell
   const long long want = pblocks > mblocks ? pblocks : mblocks;
   clear_deposit_kernel<<<(int)want, 256, 0, (cudaStream_t)stream>>>(sz * (uint32_t)p->nz, sy, sz, deposit_cells,
                                                                    order, np, pdrag, deposit_mask);
+  count_launch();
+  POG_TRY_CUDA(cudaGetLastError());
+  return POG_OK;
+}
+
+int pog_drag_from_fixed_cells(const pog_params* p, long long* pdrag_fix, const int32_t* deposit_cells, int np,
+                              const int32_t* order, float* pdrag, void* stream) {
+  int rc = pog_validate_params(p);
+  if (rc) return rc;
+  if (np < 0) return set_error(POG_E_ARG, "np=%d", np);
+  if (np == 0) return POG_OK;
+  if (!pdrag_fix || !deposit_cells || !pdrag) return set_error(POG_E_ARG, "NULL pointer");
+  const uint32_t sy = (uint32_t)p->nx, sz = (uint32_t)p->nx * (uint32_t)p->ny;
+  fixed_to_float_cells_kernel<<<(np + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
+      sz * (uint32_t)p->nz, sy, sz, deposit_cells, order, np, (unsigned long long*)pdrag_fix, pdrag);
   count_launch();
   POG_TRY_CUDA(cudaGetLastError());
   return POG_OK;

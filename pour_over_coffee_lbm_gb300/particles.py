@@ -161,10 +161,9 @@ class CoffeeParticleSystem:
         f_out = pdrag if pdrag is not None else solver._pdrag
         fix = None
         if pc.deterministic:
+            # all zeros between passes: each pass's conversion takes back every entry it deposited
             if self._fix is None or self._fix.numel() != 4 * solver.n:
                 self._fix = torch.zeros(4 * solver.n, dtype=torch.int64, device=self.device)
-            else:
-                self._fix.zero_()
             fix = self._fix
         s = _lib.stream_handle()
         _lib.check(self.lib.pog_particles_couple(
@@ -173,9 +172,8 @@ class CoffeeParticleSystem:
             _lib.ptr(solver._u), None if pc.deterministic else _lib.ptr(f_out), _lib.ptr(fix),
             _lib.ptr(self._u_at), s))
         if pc.deterministic:
-            tmp = torch.empty_like(f_out)
-            _lib.check(self.lib.pog_drag_from_fixed(solver._p, _lib.ptr(fix), _lib.ptr(tmp), s))
-            f_out.add_(tmp)
+            _lib.check(self.lib.pog_drag_from_fixed_cells(solver._p, _lib.ptr(fix), _lib.ptr(self._dep), n,
+                                                          _lib.ptr(self._perm), _lib.ptr(f_out), s))
         self._solver = solver
         self._since_sort = (self._since_sort or 0) + 1
         self._dep_n = n

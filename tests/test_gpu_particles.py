@@ -148,3 +148,43 @@ def test_couple_nonfinite_deactivates(cuda, orc):
     o = orc.particles_couple(cfg, pc, pos, vel, d, np.zeros_like(pos), act, u)
     assert g[3][5] == 0 and o[3][5] == 0
     assert np.array_equal(g[3], o[3])
+
+
+@pytest.mark.parametrize("sorted_order", [False, True])
+def test_drag_from_fixed_cells_equals_full_conversion(cuda, orc, sorted_order):
+    """pog_drag_from_fixed_cells converts the deterministic deposit at the particles' cells only:
+    added to a field that already holds values, it gives exactly that field plus
+    pog_drag_from_fixed's conversion, and it leaves the fixed-point field all zeros (20,000
+    particles on 128^3, many sharing cells)."""
+    rng = np.random.default_rng(5)
+    cfg = LatticeConfig(nx=128, ny=128, nz=128, band_thickness=3.0)
+    pc = ParticleConfig(count=20000)
+    pos, vel, d, act = seed_particles(cfg, pc)
+    act[::97] = 0
+    u = torch.as_tensor(_flow(cfg, rng)).cuda()
+    n = d.shape[0]
+    p = cfg.to_c()
+    pp = pc.to_c()
+    pp.deterministic = 1
+    dep = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    pp.deposit_cells = dep.data_ptr()
+    T = lambda a, dt=np.float32: torch.as_tensor(np.ascontiguousarray(a, dt)).cuda()  # noqa: E731
+    pos_t, vel_t, d_t, act_t = T(pos), T(vel), T(d), T(act, np.int32)
+    drag_t = torch.zeros_like(vel_t)
+    order = None
+    if sorted_order:
+        _, o = orc.particles_bin(cfg, pos, act)
+        order = T(o, np.int32)
+    fix = torch.zeros(4 * cfg.ncell, dtype=torch.int64, device="cuda")
+    _lib.check(lib().pog_particles_couple(ctypes.byref(p), ctypes.byref(pp), P(pos_t), P(vel_t), P(d_t), P(drag_t),
+                                          P(act_t), n, P(order), P(u), None, P(fix), None, S()))
+    base = torch.randn(4 * cfg.ncell, device="cuda")  # values already in the field
+    full = torch.empty_like(base)
+    _lib.check(lib().pog_drag_from_fixed(ctypes.byref(p), P(fix), P(full), S()))
+    cells = base.clone()
+    _lib.check(lib().pog_drag_from_fixed_cells(ctypes.byref(p), P(fix), P(dep), n, P(order), P(cells), S()))
+    torch.cuda.synchronize()
+    assert int((dep >= 0).sum()) > 0 and int((dep == -7).sum()) == 0
+    assert int(torch.count_nonzero(full)) > 0
+    assert torch.equal(cells, base + full)
+    assert int(torch.count_nonzero(fix)) == 0
