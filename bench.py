@@ -488,7 +488,9 @@ def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="auto"):
     per_step = el / timed
     fwd_bytes = (77 + 16) * cfg.ncell + 268 * pc.count
     fwd_gbs = fwd_bytes / per_step / 1e9
-    del g, s, ps
+    del g
+    particles = particle_pass(s, ps, peak)
+    del s, ps
     torch.cuda.empty_cache()
     run = OutflowAdjoint(cfg.replace(storage=STORE_F32), adj_steps, ckpt)
     # gradients w.r.t. the band's per-cell porosity (the inlet is more than adj_steps planes
@@ -511,6 +513,7 @@ def scale_row(steps, peak, adj_steps=200, ckpt=20, step_kernel="auto"):
            "coupled_roofline": {"algorithmic_bytes_per_step": fwd_bytes, "achieved_gbs": round(fwd_gbs, 1),
                                 "frac": round(fwd_gbs / peak[0], 4), "peak": peak[0], "peak_source": peak[1],
                                 "bytes": "77 B per cell update (FP16S) + 16 B rho/u write + 268 B per particle"},
+           "particle_pass": particles,
            "adjoint": {"steps": adj_steps, "forward_ms": round(fwd * 1e3, 1), "backward_ms": round(bwd * 1e3, 1),
                        "adjoint_mlups": round(cfg.ncell * adj_steps / bwd / 1e6, 1), "loss": J,
                        "roofline": {"achieved_gbs": round(adj_gbs, 1), "frac": round(adj_gbs / peak[0], 4),
@@ -794,6 +797,31 @@ def headline(args, peak, world, local):
     return out
 
 
+def particle_pass(solver, ps, peak, reps=10):
+    """The coupling pass alone (couple_kernel: trilinear gather, drag, relaxation, integration with
+    the cone constraint, deposit), `reps` passes on the current state into a scratch deposit field,
+    timed with CUDA events between two particle sorts: 268 B per active particle (8 x 12 B u
+    gathers, 8 x 12 B deposit, position / velocity / drag state read and written, diameter),
+    reported as its own particle GB/s beside the lattice's."""
+    import torch
+    scratch = torch.zeros_like(solver._pdrag)
+    mask = torch.zeros_like(solver._dmask)
+    for _ in range(3):
+        ps.couple(solver, pdrag=scratch, deposit_mask=mask)
+    ps._since_sort = 0  # no sort inside the timed passes (sort_interval > reps)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    for _ in range(reps):
+        ps.couple(solver, pdrag=scratch, deposit_mask=mask)
+    ev[1].record()
+    torch.cuda.synchronize()
+    us = ev[0].elapsed_time(ev[1]) * 1e3 / reps
+    active = int((ps._active[:ps.count] != 0).sum().item())
+    gbs = 268 * active / us / 1e3
+    return {"kernel": "couple_kernel (one coupling pass)", "us_per_pass": round(us, 2), "active_particles": active,
+            "bytes_per_particle": 268, "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak[0], 4)}
+
+
 def coupled_line(args, peak):
     """The 128^3 two-way coupled case (20,000 particles): graph-replayed steps, the public-API
     coupled step end to end, and the step kernel's roofline."""
@@ -838,6 +866,7 @@ def coupled_line(args, peak):
     e2e_ok = bool(torch.isfinite(red_h[:, :5]).all()) and float(red_h[:, 5].sum()) == 0.0
     solver.set_inlet_control(None)
     diag = solver.get_diagnostics()
+    particles = particle_pass(solver, ps, peak)
     out = {"workload": "coupled FP32: %dx%dx%d D3Q19, LES Cs 0.1 (local strain), porous band 3 cells (eps 0.6, "
                        "K 1e-3, C_F 0.55), %d log-normal particles two-way coupled; a step = coupling pass + "
                        "lattice step" % (cfg.nx, cfg.ny, cfg.nz, pc.count),
@@ -847,7 +876,7 @@ def coupled_line(args, peak):
            "e2e": {"value": round(cfg.ncell * K / e2e_el / 1e6, 1), "unit": "MLUPS", "h2d_bytes_per_step": 68,
                    "d2h_bytes_per_step": 48, "results_finite": e2e_ok,
                    "api": "GB300LBMSolver.step_with_two_way_coupling(reduce=True) per step"},
-           "stable": diag["stable"],
+           "stable": diag["stable"], "particle_pass": particles,
            "l2": "distributions %.0f MB > 129 MB L2 (no flush)" % (19 * 4 * cfg.ncell / 1e6)}
     del graph, solver, ps
     torch.cuda.empty_cache()
