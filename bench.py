@@ -919,7 +919,7 @@ def run_ours(args):
             h["roofline"]["traffic"] = tr[key]["bytes_per_step"]
             h["roofline"]["traffic_source"] = tr[key].get("source")
 
-    extra = coupled = rows = diff = scale = None
+    extra = coupled = rows = diff = scale = adj = None
     if not args.no_extra and not args.small and rank == 0:
         from pour_over_coffee_lbm_gb300.params import STORE_BF16S, STORE_F16S, STORE_F32
         extra = {}
@@ -940,6 +940,7 @@ def run_ours(args):
         coupled = coupled_line(args, peak)
         rows = plugin_rows(*workload(False), 200, peak)
         diff = differentiation_rows(peak)
+        adj = adjoint_line(256, 20, peak)
         if args.scale_steps > 0:
             scale = scale_row(args.scale_steps, peak, step_kernel=args.step_kernel)
 
@@ -971,6 +972,7 @@ def run_ours(args):
             "coupled_128": coupled,
             "plugin_rows": rows,
             "differentiation_96": diff,
+            "adjoint_256": adj,
             "scale_320x320x384": scale,
         }
         print(json.dumps(line), flush=True)
@@ -1034,10 +1036,10 @@ def run_coupled_only(args):
     print(json.dumps({"coupled_only": coupled_line(args, peaks())}), flush=True)
 
 
-def run_adjoint_only(args):
+def adjoint_line(N, calls, peak):
     """The adjoint step (pog_adjoint_step: adjoint_kernel + the inlet-plane pass) alone on an N^3
     FP32 LES(local) + porous-band lattice with a porosity field, on a recomputed forward state:
-    `--steps` calls timed with CUDA events after 3 warm-up calls.  Algorithmic bytes per call:
+    `calls` calls timed with CUDA events after 3 warm-up calls.  Algorithmic bytes per call:
     232 B per non-solid cell (f_t, lam_{t+1} and lam_t, 19 x 4 B each, and the flag word), 80 B
     per solid cell (flag word, lam_t zeroed), and 20 B more per porous cell (porosity, the FP64
     porosity gradient read and written)."""
@@ -1046,8 +1048,6 @@ def run_adjoint_only(args):
     from pour_over_coffee_lbm_gb300.adjoint import OutflowAdjoint
     from pour_over_coffee_lbm_gb300.params import CELL_POROUS, CELL_SOLID, LES_LOCAL, STORE_F32, LatticeConfig, \
         porosity_field
-    torch.cuda.set_device(0)
-    N = args.adjoint_only
     cfg = LatticeConfig(nx=N, ny=N, nz=N, band_thickness=3.0, les_mode=LES_LOCAL, storage=STORE_F32, u_inlet=-0.05)
     run = OutflowAdjoint(cfg, 8, 4)
     fl = run.flags.cpu().numpy()
@@ -1070,20 +1070,30 @@ def run_adjoint_only(args):
     torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ev[0].record()
-    for _ in range(args.steps):
+    for _ in range(calls):
         call()
     ev[1].record()
     torch.cuda.synchronize()
-    us = ev[0].elapsed_time(ev[1]) * 1e3 / args.steps
+    us = ev[0].elapsed_time(ev[1]) * 1e3 / calls
     solid = int(((run.flags & CELL_SOLID) != 0).sum().item())
     porous = int((((run.flags & CELL_POROUS) != 0) & ((run.flags & CELL_SOLID) == 0)).sum().item())
     nbytes = 232 * (cfg.ncell - solid) + 80 * solid + 20 * porous
-    peak = peaks()
     gbs = nbytes / us / 1e3
-    print(json.dumps({"adjoint_only": N, "calls": args.steps, "us_per_call": round(us, 1),
-                      "mlups": round(cfg.ncell / us, 1), "algorithmic_bytes": nbytes, "achieved_gbs": round(gbs, 1),
-                      "frac": round(gbs / peak[0], 4), "peak_source": peak[1],
-                      "finite": bool(torch.isfinite(lam_t).all())}), flush=True)
+    out = {"workload": "adjoint step alone, %d^3 FP32 LES(local) + porous band with a porosity field" % N,
+           "calls": calls, "us_per_call": round(us, 1), "mlups": round(cfg.ncell / us, 1),
+           "algorithmic_bytes": nbytes, "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak[0], 4),
+           "peak_source": peak[1], "finite": bool(torch.isfinite(lam_t).all()),
+           "bytes": "232 B per fluid cell, 80 per solid cell, +20 per porous cell"}
+    del run, lam, lam_t, g_eps
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_adjoint_only(args):
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps({"adjoint_only": args.adjoint_only, **adjoint_line(args.adjoint_only, args.steps, peaks())}),
+          flush=True)
 
 
 def main():
